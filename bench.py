@@ -1,0 +1,448 @@
+#!/usr/bin/env python
+"""bench.py -- throughput of the batched best-first graph search on GB300.
+
+One step = one batched search of the workload's query set (10,000 queries)
+over the resident index.  Default workload: 1,000,000 x 128 float32 vectors
+with integer values 0-255 (1,000-centre Gaussian mixture, sigma 20; a
+synthetic stand-in for SIFT1M's shape), L2, degree-32 graph (shift 5,
+FIXED_DEGREE 31, SEARCH_DEGREE 15) built by this project's batch-parallel
+builder, pq_size chosen as the smallest in a sweep whose recall@10 against an
+FP64 exact kNN reaches the target (0.95), top-10 returned.
+
+  value  queries/s of the kernel, queries and index resident in HBM, CUDA
+         events on the launching stream, L2 flushed between steps.
+  e2e    queries/s through song_search (host query buffer in pinned memory,
+         host->device copy, search, device->host copy of the ids), host clock.
+
+`--impl reference` times the reference's CPU best-first search
+(graph.h:169-216; the oracle's restatement, pinned to the reference's own
+code by tests/golden) on all host cores, at the result size k whose recall@10
+matches the target, on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PQ_SWEEP = [50, 100, 150, 200, 250, 300, 350, 400, 500, 600, 800, 1000]
+CPU_K_SWEEP = [10, 15, 20, 30, 40, 60, 80, 100, 150, 200, 300]
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", default="scale-1m-128d-l2")
+    p.add_argument("--pq", type=int, default=0, help="0 = smallest pq reaching --recall")
+    p.add_argument("--recall", type=float, default=0.95)
+    p.add_argument("--topk", type=int, default=10)
+    p.add_argument("--nq", type=int, default=0)
+    p.add_argument("--build-div", type=int, default=64)
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cache", default=os.environ.get("SONG_CACHE", "/tmp/song_gb300_cache"))
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def load_workload(args, rank=0, barrier=None):
+    import song_gb300 as S
+    from song_gb300 import datasets as D
+    w = D.WORKLOADS[args.workload]
+    nq = args.nq or w.n_queries
+    t = time.time()
+    data = D.base_vectors(w)
+    queries = D.query_vectors(w, nq=nq)
+    log("[bench] %s: data %s queries %s in %.1fs" % (w.name, data.shape, queries.shape, time.time() - t))
+    os.makedirs(args.cache, exist_ok=True)
+    gpath = os.path.join(args.cache, "%s.div%d.graph" % (w.name, args.build_div))
+    if rank == 0 and not os.path.exists(gpath):
+        t = time.time()
+        g = S.graph_build(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
+                          batch_div=args.build_div, nthreads=os.cpu_count())
+        tmp = gpath + ".tmp%d" % os.getpid()
+        g.tofile(tmp)
+        os.replace(tmp, gpath)
+        log("[bench] graph built in %.1fs (batch_div %d, %d threads)" % (time.time() - t, args.build_div, os.cpu_count()))
+    if barrier:
+        barrier()
+    graph = np.fromfile(gpath, dtype=np.uint64)
+    return w, data, queries, graph
+
+
+def ground_truth(args, w, data, queries, k):
+    from song_gb300 import groundtruth as GT
+    path = os.path.join(args.cache, "%s.nq%d.k%d.gt.npz" % (w.name, queries.shape[0], k))
+    if os.path.exists(path):
+        z = np.load(path)
+        return z["ids"], z["kth"]
+    t = time.time()
+    ids, kth = GT.exact_knn_fp64(data, queries, k, w.metric)
+    np.savez(path, ids=ids, kth=kth)
+    log("[bench] fp64 exact kNN in %.1fs" % (time.time() - t))
+    return ids, kth
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+REASON_FIELDS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap,utilization.gpu")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        return self.summary()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        loaded = [r for r in self.rows if num(r[7]) and num(r[7]) > 0] or self.rows
+        sm = [num(r[0]) for r in loaded if num(r[0]) is not None]
+        mx = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        reasons = set()
+        for r in loaded:
+            for name, v in zip(REASON_FIELDS, r[3:7]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows), "samples_under_load": len(loaded)}
+
+
+# ---------------------------------------------------------------------------
+# CPU reference search (oracle restatement of graph.h:169-216)
+# ---------------------------------------------------------------------------
+
+def cpu_calibrate_k(w, data, graph, queries, target, gt_ids, gt_kth, sample=400):
+    from oracle import oracle as O
+    from song_gb300 import groundtruth as GT
+    ox = O.OracleIndex(data, graph, w.shift, O.METRICS[w.metric])
+    qs = queries[:sample]
+    sweep = []
+    for k in CPU_K_SWEEP:
+        if k < 10:
+            continue
+        ids, _ = ox.cpu_search(qs, k)
+        r = GT.recall_tie_aware(ids, data, qs, gt_kth[:sample], w.metric, 10)
+        sweep.append((k, round(r, 4)))
+        if r >= target:
+            return k, sweep
+    return CPU_K_SWEEP[-1], sweep
+
+
+def cpu_time(w, data, graph, queries, k, seconds, nthreads):
+    """Times the CPU search on a sample sized to about `seconds` of work."""
+    from oracle import oracle as O
+    ox = O.OracleIndex(data, graph, w.shift, O.METRICS[w.metric])
+    pilot = queries[:max(64, 8 * nthreads)]
+    t = time.perf_counter()
+    ox.cpu_search(pilot, k, nthreads=nthreads)
+    rate = pilot.shape[0] / max(1e-6, time.perf_counter() - t)
+    n = int(min(max(256, rate * seconds), 200_000))
+    idx = np.arange(n) % queries.shape[0]
+    sample = queries[idx]
+    t = time.perf_counter()
+    ox.cpu_search(sample, k, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    return n / dt, n, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU search on all host cores."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    w, data, queries, graph = load_workload(args)
+    from song_gb300 import groundtruth as GT
+    sample = min(400, queries.shape[0])
+    gt_ids, gt_kth = GT.exact_knn_fp64(data, queries[:sample], args.topk, w.metric, device="cpu")
+    k, sweep = cpu_calibrate_k(w, data, graph, queries, args.recall, gt_ids, gt_kth, sample)
+    nthreads = os.cpu_count() or 1
+    per_step = max(1.0, 150.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_time(w, data, graph, queries, k, per_step / 4, nthreads)
+    total_q, total_t = 0, 0.0
+    for _ in range(args.steps):
+        rate, n, dt = cpu_time(w, data, graph, queries, k, per_step, nthreads)
+        total_q += n
+        total_t += dt
+    value = total_q / total_t
+    line = {
+        "impl": "reference", "metric": "queries/s at recall@10>=%.2f" % args.recall, "value": round(value, 1),
+        "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64-accumulated f32", "data": "synthetic",
+        "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric, "graph_shift": w.shift,
+                   "search": "CPU best-first search graph.h:169-216 (oracle restatement)",
+                   "k": k, "recall_sweep_k": sweep, "queries_per_step": total_q // args.steps},
+        "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d queries per step (workload query set repeated), k=%d" % (total_q // args.steps, k)},
+        "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# ours
+# ---------------------------------------------------------------------------
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    import song_gb300 as S
+    from song_gb300 import groundtruth as GT
+    S.load_library()
+    w, data, queries, graph = load_workload(args, rank, barrier)
+    nq, k = queries.shape[0], args.topk
+    gt_ids, gt_kth = ground_truth(args, w, data, queries, k)
+
+    t = time.time()
+    ix = S.Index(graph, data, w.shift, w.metric, device=local)
+    log("[bench] index resident (%.2f GB) in %.1fs" % (ix.device_bytes() / 1e9, time.time() - t))
+
+    dq = torch.from_numpy(queries).cuda()
+    dout = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+    dhops = torch.empty(nq, dtype=torch.int32, device="cuda")
+    devals = torch.empty(nq, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def search(pq, stats=False):
+        ix.search_device(dq.data_ptr(), nq, pq, k, dout.data_ptr(),
+                         dhops.data_ptr() if stats else None, devals.data_ptr() if stats else None, sh)
+
+    # pq sweep: smallest pq whose tie-aware recall@10 reaches the target
+    sweep = []
+    pq = args.pq
+    if pq == 0:
+        for cand in PQ_SWEEP:
+            search(cand)
+            torch.cuda.synchronize()
+            ids = dout.cpu().numpy().view(np.uint64)
+            r = GT.recall_tie_aware(ids, data, queries, gt_kth, w.metric, k)
+            sweep.append([cand, round(r, 4)])
+            log("[bench] pq %d recall@10 %.4f" % (cand, r))
+            if r >= args.recall:
+                pq = cand
+                break
+        if pq == 0:
+            pq = PQ_SWEEP[-1]
+    search(pq, stats=True)
+    torch.cuda.synchronize()
+    ids = dout.cpu().numpy().view(np.uint64)
+    rec = GT.recall_tie_aware(ids, data, queries, gt_kth, w.metric, k)
+    rec_ids = GT.recall(ids, gt_ids, k)
+    hops = dhops.cpu().numpy().astype(np.int64)
+    evals = devals.cpu().numpy().astype(np.int64)
+
+    # L2 flush buffer (larger than the 129 MB L2)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    # warm-up: at least W steps and at least ~1.5 s so the clock sampler sees load
+    t0 = time.time()
+    wsteps = 0
+    while wsteps < args.warmup or time.time() - t0 < 1.5:
+        flush.zero_()
+        search(pq)
+        wsteps += 1
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        search(pq)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier()
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(kernel_ms) / 1000.0
+    if dist:
+        tt = torch.tensor([total_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_s = float(tt.item())
+    value = world * nq * args.steps / total_s
+
+    # e2e: host buffers through song_search (pinned query buffer)
+    pinned = torch.empty((nq, w.dim), dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = queries
+    hq = pinned.numpy()
+    out_host = torch.empty((nq, k), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    import ctypes
+    L = S.load_library()
+    for _ in range(max(1, args.warmup)):
+        S._check(L.song_search(ix._h, hq.ctypes.data_as(ctypes.c_void_p), nq, pq, k,
+                               out_host.ctypes.data_as(ctypes.c_void_p), None, None))
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        S._check(L.song_search(ix._h, hq.ctypes.data_as(ctypes.c_void_p), nq, pq, k,
+                               out_host.ctypes.data_as(ctypes.c_void_p), None, None))
+        e2e_times.append(time.perf_counter() - t)
+    clocks = sampler.stop()
+    assert np.array_equal(out_host, ids), "e2e results differ from the device-buffer results"
+    e2e_s = sum(e2e_times)
+    if dist:
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = world * nq * args.steps / e2e_s
+
+    # roofline: algorithmic bytes per launch / mean kernel time
+    row_bytes = 4 * ((w.dim + 3) // 4)
+    alg_bytes = int((4 * w.dim * nq) + hops.sum() * (1 << w.shift) * 4 + evals.sum() * row_bytes + nq * k * 8)
+    mean_s = (sum(kernel_ms) / len(kernel_ms)) / 1000.0
+    achieved = alg_bytes / mean_s / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_scale.json")
+    if os.path.exists(tp):
+        try:
+            tj = json.load(open(tp))
+            if tj.get("pq") == pq and tj.get("workload") == w.name:
+                traffic = tj.get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            from oracle import oracle as O
+            O.build()
+            sample = min(400, nq)
+            ck, csweep = cpu_calibrate_k(w, data, graph, queries, args.recall, gt_ids, gt_kth, sample)
+            nthreads = os.cpu_count() or 1
+            rate, n, dt = cpu_time(w, data, graph, queries, ck, args.cpu_seconds, nthreads)
+            cpu = {"value": round(rate, 1), "unit": "queries/s", "cores": nthreads, "kind": "port",
+                   "sample": "%d queries (workload set repeated), k=%d for recall@10>=%.2f, %.1fs" % (n, ck, args.recall, dt),
+                   "recall_sweep_k": csweep}
+        except Exception as e:  # the baseline must not hide the GPU number
+            cpu = {"value": None, "error": repr(e)}
+
+    if rank == 0:
+        line = {
+            "metric": "queries/s at recall@10>=%.2f, %s (plain FP32 search)" % (args.recall, w.name),
+            "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": wsteps, "ms_per_step": round(1000 * total_s / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian mixture, SIFT1M shape)",
+            "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric,
+                       "graph": "shift %d (FIXED_DEGREE %d, SEARCH_DEGREE %d), batch-parallel build div %d"
+                                % (w.shift, w.fixed_degree, w.search_degree, args.build_div),
+                       "pq": pq, "top_k": k, "queries_per_step": nq, "recall_at_10": round(rec, 4),
+                       "recall_at_10_ids": round(rec_ids, 4), "pq_sweep": sweep,
+                       "mean_hops": round(float(hops.mean()), 2), "mean_evals": round(float(evals.mean()), 2),
+                       "l2": "flushed between steps (256 MB write); index 512 MB > L2",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(nq * w.dim * 4),
+                    "d2h_bytes_per_step": int(nq * k * 8)},
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+            "kernel_ms": {"min": round(min(kernel_ms), 4), "median": round(statistics.median(kernel_ms), 4),
+                          "max": round(max(kernel_ms), 4)},
+            "wall_s_timed": round(wall, 4),
+        }
+        print(json.dumps(line), flush=True)
+    ix.free()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

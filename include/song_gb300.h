@@ -1,0 +1,131 @@
+/*
+ * song_gb300.h -- C ABI of the GB300 (sm_103a) batched best-first graph search.
+ *
+ * A drop-in for the GPU search path of sunbelbd/song:
+ *
+ *   GraphWrapper::search_top_k_batch(queries, k, results)          kernelgraph.h:20, :269-272
+ *     -> WarpAStarAccelerator::astar_multi_start_search_batch(
+ *            queries, k, results, h_data, h_graph, vertex_offset_shift, num, dim)
+ *                                                                   warp_astar_accelerator.h:347-423
+ *     -> warp_independent_search_kernel<<<nq, 32>>>(...)            warp_astar_accelerator.h:41-341
+ *
+ * Inputs are the reference's own formats: base vectors as bfsg.data (n x dim
+ * float32, row-major; data.h:164-175) and the graph as bfsg.graph (n << shift
+ * uint64 slots, slot 0 = out-degree, then zero-based neighbour ids;
+ * README.md:83-89, kernelgraph.h:255-267).  Results are zero-based ids in
+ * ascending distance order, the first k of the pq_size best, as the
+ * reference CLI prints them (main.cu:28-32).
+ *
+ * The reference fixes pq_size (TOPK), dim (DIM) and the metric at compile
+ * time (fill_parameters.sh:35-65); here they are run-time arguments.
+ *
+ * Every call returns a status code.  An index is uploaded once and stays
+ * resident.  One index may be searched from one host thread at a time; a
+ * search is ordered on the stream it is given.
+ */
+#ifndef SONG_GB300_H
+#define SONG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference has no error reporting at all
+ * (warp_astar_accelerator.h:353-423 checks no CUDA call). */
+#define SONG_OK 0
+#define SONG_ERR_ARG 1     /* an argument is out of range or the graph is malformed */
+#define SONG_ERR_OOM 2     /* device or host allocation failed                    */
+#define SONG_ERR_TIMEOUT 3 /* a bounded device wait gave up                       */
+#define SONG_ERR_CUDA 4    /* a CUDA runtime call failed                          */
+#define SONG_ERR_IO 5      /* a file could not be opened or was too short         */
+
+/* Metrics: the reference's __USE_L2_DIST / __USE_IP_DIST / __USE_COS_DIST
+ * (Makefile:3, fill_parameters.sh:55-65), in KernelFixedDegreeGraph<0|1|2>
+ * order (main.cu:66-75).  L2 = squared Euclidean; IP = negative inner
+ * product; COS = -sign(q.x) (q.x)^2 / |x|^2 as the GPU kernel computes it
+ * (warp_astar_accelerator.h:275-281). */
+#define SONG_METRIC_L2 0
+#define SONG_METRIC_IP 1
+#define SONG_METRIC_COS 2
+
+/* Device storage of the base vectors.  F32 is the reference's value_t
+ * (config.h:11).  BF16 and FP8 (E4M3 with one float scale per vector) are
+ * additions with no counterpart in the reference; their final candidates are
+ * re-ranked with FP32 distances. */
+#define SONG_STORAGE_F32 0
+#define SONG_STORAGE_BF16 1
+#define SONG_STORAGE_FP8 2
+
+/* Limits of this implementation. */
+#define SONG_MAX_PQ 1023   /* the reference's FixHash casts its slot to short: 8*pq < 32768 */
+#define SONG_MAX_SHIFT 5   /* up to 31 neighbours per vertex, as FIXED_DEGREE (config.h:22) */
+
+typedef struct song_index song_index;
+
+/* Human-readable text of a status code. */
+const char *song_status_string(int status);
+
+/* Text of the last error raised on the calling host thread ("" if none). */
+const char *song_last_error(void);
+
+/* Create a resident index on CUDA device `device` from host arrays in the
+ * reference layouts.  `graph` has n << shift uint64 entries; every degree must
+ * be <= (1 << shift) - 1 and every neighbour id < n.  `data` is n x dim.
+ * Replaces the per-call upload of warp_astar_accelerator.h:353-356. */
+int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int dim, int shift,
+                      int metric, int storage, int device, song_index **out);
+
+/* The same from bfsg.graph / bfsg.data files (kernelgraph.h:262-267,
+ * data.h:170-175).  As in the reference, n and dim are not stored in the
+ * files and must be given. */
+int song_index_load(const char *graph_path, const char *data_path, uint64_t n, int dim, int shift,
+                    int metric, int storage, int device, song_index **out);
+
+int song_index_free(song_index *index);
+
+/* Properties of an index (any pointer may be NULL). */
+int song_index_info(const song_index *index, uint64_t *n, int *dim, int *shift, int *metric,
+                    int *storage, uint64_t *device_bytes);
+
+/* Batched search with HOST buffers: copies nq x dim float queries to the
+ * device, searches, copies nq x k uint64 ids back, and returns when done.
+ * 2 <= pq <= SONG_MAX_PQ, 1 <= k <= pq.  hops and evals (nq int32 each) may be
+ * NULL; they receive per query the number of vertices expanded and of
+ * distances computed.  This is the e2e call that replaces
+ * astar_multi_start_search_batch (warp_astar_accelerator.h:347). */
+int song_search(song_index *index, const float *queries, int nq, int pq, int k, uint64_t *out,
+                int32_t *hops, int32_t *evals);
+
+/* Batched search with DEVICE buffers, enqueued on `stream` (a cudaStream_t,
+ * NULL = the legacy default stream) without synchronising. */
+int song_search_device(song_index *index, const float *d_queries, int nq, int pq, int k,
+                       uint64_t *d_out, int32_t *d_hops, int32_t *d_evals, void *stream);
+
+/* One-shot form with the reference's own argument list
+ * (warp_astar_accelerator.h:347): uploads data and graph, searches, frees.
+ * results: nq x pq ids, as d_result (warp_astar_accelerator.h:334).  The
+ * reference's `k` argument is ignored there and has no counterpart here. */
+int song_astar_search_batch(const float *queries, int nq, int pq, uint64_t *results,
+                            const float *h_data, const uint64_t *h_graph, int vertex_offset_shift,
+                            uint64_t num, int dim, int metric);
+
+/* Graph construction (graph.h:149-167 with config.h:22-27 constants as
+ * arguments): fills graph_out (n << shift uint64) in the bfsg.graph layout.
+ * batch_div = 0 reproduces the reference's sequential insertion exactly;
+ * batch_div > 0 inserts in deterministic parallel batches of
+ * max(1, inserted / batch_div) vertices on nthreads host threads. */
+int song_graph_build(const float *data, uint64_t n, int dim, int metric, int shift,
+                     int search_degree, int fixed_degree, int budget, int batch_div, int nthreads,
+                     uint64_t *graph_out);
+
+/* The visited-hash slot function of the reference's default build
+ * (fixhash.h:20-24) evaluated on the device for `count` ids, for tests. */
+int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SONG_GB300_H */

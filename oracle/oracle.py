@@ -1,0 +1,309 @@
+"""Python view of the CPU oracle (oracle/song_oracle.c) and of the reference
+harness (oracle/ref_harness.cpp -> oracle/_ref/).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
+the cpu_baseline / reference legs of bench.py, always as the checker or the
+timed CPU baseline, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libsong_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+L2, IP, COS = 0, 1, 2
+METRICS = {"l2": L2, "ip": IP, "cos": COS}
+MODE_REF, MODE_LEX = 0, 1
+NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+EV_NAMES = {1: "POP", 2: "FINISH", 3: "TEVICT", 4: "SKIP", 5: "INSERT", 6: "QEVICT", 7: "TEST",
+            8: "OUT"}
+
+
+class _Index(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("graph", ctypes.c_void_p), ("n", ctypes.c_uint64),
+                ("dim", ctypes.c_int32), ("shift", ctypes.c_int32), ("metric", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+
+EVENT_DTYPE = np.dtype([("kind", np.int32), ("pad", np.uint32), ("id", np.uint64),
+                        ("dist", np.float32), ("pad2", np.uint32)])
+
+
+def build(force: bool = False) -> str:
+    """Compile song_oracle.c with gcc (contraction off, portable flags)."""
+    src = os.path.join(HERE, "song_oracle.c")
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(os.path.join(HERE, "song_oracle.h"))):
+        return LIB_PATH
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math",
+                           "-fPIC", "-shared", "-pthread", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_ref() -> bool:
+    """Build oracle/_ref from the reference tree when it is present."""
+    script = os.path.join(HERE, "build_ref.sh")
+    subprocess.check_call(["bash", script])
+    return ref_available()
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        i32 = ctypes.c_int
+        L.orc_kernel_distance.restype = ctypes.c_float
+        L.orc_kernel_distance.argtypes = [i32, i32, P, P, i32]
+        L.orc_cpu_distance.restype = ctypes.c_double
+        L.orc_cpu_distance.argtypes = [i32, i32, P, P]
+        L.orc_kernel_search.restype = i32
+        L.orc_kernel_search.argtypes = [P, P, i32, i32, i32, i32, P, P, P, P, i32]
+        L.orc_kernel_search_log.restype = i32
+        L.orc_kernel_search_log.argtypes = [P, P, i32, i32, i32, P, P, i32, P]
+        L.orc_classify.restype = i32
+        L.orc_classify.argtypes = [P, i32, P, i32, P]
+        L.orc_cpu_search.restype = i32
+        L.orc_cpu_search.argtypes = [P, P, i32, i32, P, P, i32]
+        L.orc_fixhash_hash.restype = i32
+        L.orc_fixhash_hash.argtypes = [i32, ctypes.c_uint64]
+        L.orc_fixhash_init.argtypes = [P, i32]
+        L.orc_fixhash_add.argtypes = [P, i32, ctypes.c_int32]
+        L.orc_fixhash_test.restype = i32
+        L.orc_fixhash_test.argtypes = [P, i32, ctypes.c_int32]
+        L.orc_fixhash_del.argtypes = [P, i32, ctypes.c_int32]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def default_threads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+class OracleIndex:
+    """Holds host arrays in the reference's file layouts (bfsg.data: n x dim f32;
+    bfsg.graph: n << shift uint64, slot 0 = degree)."""
+
+    def __init__(self, data: np.ndarray, graph: np.ndarray, shift: int, metric: int):
+        self.data = np.ascontiguousarray(data, dtype=np.float32)
+        self.graph = np.ascontiguousarray(graph, dtype=np.uint64).reshape(-1)
+        self.n, self.dim = self.data.shape
+        self.shift = int(shift)
+        self.metric = int(metric)
+        assert self.graph.size == self.n << self.shift
+        self._s = _Index(self.data.ctypes.data, self.graph.ctypes.data, self.n, self.dim,
+                         self.shift, self.metric, 0)
+
+    @property
+    def ref(self):
+        return ctypes.byref(self._s)
+
+    def kernel_search(self, queries, pq, mode=MODE_LEX, use_fma=True, nthreads=None):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        out = np.empty((nq, pq), dtype=np.uint64)
+        hops = np.empty(nq, dtype=np.int32)
+        evals = np.empty(nq, dtype=np.int32)
+        popped = np.empty(nq, dtype=np.int32)
+        rc = lib().orc_kernel_search(self.ref, _ptr(q), nq, pq, mode, int(use_fma), _ptr(out),
+                                     _ptr(hops), _ptr(evals), _ptr(popped),
+                                     nthreads or default_threads())
+        if rc != 0:
+            raise ValueError("orc_kernel_search failed")
+        return out, hops, evals, popped
+
+    def kernel_search_log(self, query, pq, mode, use_fma=True, cap=1 << 18):
+        q = np.ascontiguousarray(query, dtype=np.float32).reshape(-1)
+        out = np.empty(pq, dtype=np.uint64)
+        log = np.zeros(cap, dtype=EVENT_DTYPE)
+        n = ctypes.c_int(0)
+        rc = lib().orc_kernel_search_log(self.ref, _ptr(q), pq, mode, int(use_fma), _ptr(out),
+                                         _ptr(log), cap, ctypes.byref(n))
+        if rc != 0:
+            raise ValueError("orc_kernel_search_log failed")
+        if n.value > cap:
+            raise ValueError("event log overflow")
+        return out, log[:n.value]
+
+    def cpu_search(self, queries, k, nthreads=None):
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        out = np.empty((nq, k), dtype=np.uint64)
+        ex = np.empty(nq, dtype=np.int32)
+        rc = lib().orc_cpu_search(self.ref, _ptr(q), nq, k, _ptr(out), _ptr(ex),
+                                  nthreads or default_threads())
+        if rc != 0:
+            raise ValueError("orc_cpu_search failed")
+        return out, ex
+
+
+def classify(log_a, log_b):
+    """0 identical, 1 first difference is a float tie, 2 anything else; and the
+    index of the first difference (-1 if none)."""
+    at = ctypes.c_int(-1)
+    a = np.ascontiguousarray(log_a)
+    b = np.ascontiguousarray(log_b)
+    r = lib().orc_classify(_ptr(a), len(a), _ptr(b), len(b), ctypes.byref(at))
+    return r, at.value
+
+
+def kernel_distance(metric, q, x, use_fma=True):
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return lib().orc_kernel_distance(metric, q.size, _ptr(q), _ptr(x), int(use_fma))
+
+
+def cpu_distance(metric, x, q):
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return lib().orc_cpu_distance(metric, q.size, _ptr(x), _ptr(q))
+
+
+class FixHash:
+    """The visited hash of the reference's default build, on its own."""
+
+    def __init__(self, pq):
+        self.cap = 8 * pq
+        self.tab = np.empty(self.cap, dtype=np.int32)
+        lib().orc_fixhash_init(_ptr(self.tab), self.cap)
+
+    def hash(self, x):
+        return lib().orc_fixhash_hash(self.cap, x)
+
+    def add(self, x):
+        lib().orc_fixhash_add(_ptr(self.tab), self.cap, int(x))
+
+    def test(self, x):
+        return bool(lib().orc_fixhash_test(_ptr(self.tab), self.cap, int(x)))
+
+    def delete(self, x):
+        lib().orc_fixhash_del(_ptr(self.tab), self.cap, int(x))
+
+
+# ---------------------------------------------------------------------------
+# Reference harness (oracle/_ref), present only where the reference tree was
+# available at build time.
+# ---------------------------------------------------------------------------
+
+def ref_available(shift: int = 5) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libsongref_s%d.so" % shift))
+
+
+_ref_libs = {}
+
+
+def ref_lib(shift: int):
+    if shift not in _ref_libs:
+        path = os.path.join(REF_DIR, "libsongref_s%d.so" % shift)
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        i32 = ctypes.c_int
+        u64 = ctypes.c_uint64
+        L.ref_build_graph.restype = i32
+        L.ref_build_graph.argtypes = [P, u64, i32, i32, ctypes.c_char_p, ctypes.c_char_p]
+        L.ref_cpu_search.restype = i32
+        L.ref_cpu_search.argtypes = [ctypes.c_char_p, ctypes.c_char_p, u64, i32, i32, P, i32, i32, P]
+        L.ref_kernel_search.restype = i32
+        L.ref_kernel_search.argtypes = [P, P, u64, i32, i32, i32, P, i32, i32, P, P, P, P]
+        L.ref_fixhash_ops.restype = i32
+        L.ref_fixhash_ops.argtypes = [i32, P, P, i32, P]
+        L.ref_graph_shift.restype = i32
+        L.ref_graph_fixed_degree.restype = i32
+        L.ref_graph_search_degree.restype = i32
+        assert L.ref_graph_shift() == shift
+        _ref_libs[shift] = L
+    return _ref_libs[shift]
+
+
+def ref_build_graph(data: np.ndarray, shift: int, metric: int) -> np.ndarray:
+    """The reference's sequential CPU builder (graph.h:149-167)."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    n, dim = data.shape
+    with tempfile.TemporaryDirectory() as td:
+        g = os.path.join(td, "bfsg.graph").encode()
+        d = os.path.join(td, "bfsg.data").encode()
+        rc = ref_lib(shift).ref_build_graph(_ptr(data), n, dim, metric, g, d)
+        assert rc == 0
+        graph = np.fromfile(g.decode(), dtype=np.uint64)
+        back = np.fromfile(d.decode(), dtype=np.float32).reshape(n, dim)
+    assert np.array_equal(back, data)
+    return graph
+
+
+def ref_cpu_search(data, graph, shift, metric, queries, k):
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    n, dim = data.shape
+    q = np.ascontiguousarray(queries, dtype=np.float32)
+    out = np.empty((q.shape[0], k), dtype=np.uint64)
+    with tempfile.TemporaryDirectory() as td:
+        gp = os.path.join(td, "bfsg.graph")
+        dp = os.path.join(td, "bfsg.data")
+        np.ascontiguousarray(graph, dtype=np.uint64).tofile(gp)
+        data.tofile(dp)
+        rc = ref_lib(shift).ref_cpu_search(gp.encode(), dp.encode(), n, dim, metric, _ptr(q),
+                                           q.shape[0], k, _ptr(out))
+        assert rc == 0
+    return out
+
+
+def ref_kernel_search(data, graph, shift, metric, queries, pq):
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    graph = np.ascontiguousarray(graph, dtype=np.uint64)
+    n, dim = data.shape
+    q = np.ascontiguousarray(queries, dtype=np.float32)
+    nq = q.shape[0]
+    out = np.empty((nq, pq), dtype=np.uint64)
+    hops = np.empty(nq, dtype=np.int32)
+    evals = np.empty(nq, dtype=np.int32)
+    popped = np.empty(nq, dtype=np.int32)
+    rc = ref_lib(shift).ref_kernel_search(_ptr(data), _ptr(graph), n, dim, shift, metric, _ptr(q),
+                                          nq, pq, _ptr(out), _ptr(hops), _ptr(evals), _ptr(popped))
+    if rc != 0:
+        raise ValueError("pq %d not instantiated in the reference harness" % pq)
+    return out, hops, evals, popped
+
+
+def ref_fixhash_ops(pq, ops, keys):
+    """Run an add(0)/del(1)/test(2) sequence on the reference FixHash."""
+    ops = np.ascontiguousarray(ops, dtype=np.int32)
+    keys = np.ascontiguousarray(keys, dtype=np.int32)
+    res = np.empty(ops.size, dtype=np.int32)
+    rc = ref_lib(5).ref_fixhash_ops(pq, _ptr(ops), _ptr(keys), ops.size, _ptr(res))
+    if rc != 0:
+        raise ValueError("pq %d not instantiated" % pq)
+    return res
+
+
+def fixhash_ops(pq, ops, keys):
+    """The same sequence on the oracle's restatement."""
+    h = FixHash(pq)
+    res = np.full(len(ops), -1, dtype=np.int32)
+    for i, (op, k) in enumerate(zip(ops, keys)):
+        if op == 0:
+            h.add(k)
+        elif op == 1:
+            h.delete(k)
+        else:
+            res[i] = int(h.test(k))
+    return res

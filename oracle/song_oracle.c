@@ -1,0 +1,822 @@
+/*
+ * song_oracle.c -- CPU oracle for the batched best-first graph search.
+ *
+ * TEST INFRASTRUCTURE ONLY (see song_oracle.h).  Plain C11, no intrinsics, no
+ * inline assembly; compiled with -ffp-contract=off so that every fused
+ * multiply-add below is an explicit fmaf() and nothing else is contracted.
+ * Builds and gives the same results on x86-64 and aarch64.
+ */
+#include "song_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------- */
+/* Distances                                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* warp_astar_accelerator.h:115-163 (start vertex) and :237-287 (neighbours):
+ * lane l accumulates dims l, l+32, ... in order; the 32 partial sums are
+ * combined by tmp += shfl_xor(tmp, o) for o = 16, 8, 4, 2, 1, after which all
+ * lanes hold the same value.  Cosine: sign * tmp * tmp / |x|^2 in float with
+ * sign = (tmp < 0 ? 1 : -1), 0 when |x|^2 == 0; the query norm is not used. */
+float orc_kernel_distance(int metric, int dim, const float *q, const float *x, int use_fma) {
+  float t[32], l[32], nt[32], nl[32];
+  for (int lane = 0; lane < 32; ++lane) {
+    float a = 0.0f, b = 0.0f;
+    for (int j = lane; j < dim; j += 32) {
+      if (metric == ORC_L2) {
+        float d = q[j] - x[j];
+        if (use_fma) a = fmaf(d, d, a);
+        else { float p = d * d; a = a + p; }
+      } else {
+        if (use_fma) a = fmaf(q[j], x[j], a);
+        else { float p = q[j] * x[j]; a = a + p; }
+        if (metric == ORC_COS) {
+          if (use_fma) b = fmaf(x[j], x[j], b);
+          else { float p = x[j] * x[j]; b = b + p; }
+        }
+      }
+    }
+    t[lane] = a;
+    l[lane] = b;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int lane = 0; lane < 32; ++lane) {
+      nt[lane] = t[lane] + t[lane ^ off];
+      nl[lane] = l[lane] + l[lane ^ off];
+    }
+    memcpy(t, nt, sizeof t);
+    memcpy(l, nl, sizeof l);
+  }
+  if (metric == ORC_L2) return t[0];
+  if (metric == ORC_IP) return -t[0];
+  if (l[0] != 0.0f) {
+    float sign = t[0] < 0.0f ? 1.0f : -1.0f;
+    float st = sign * t[0];
+    float num = st * t[0];
+    return num / l[0];
+  }
+  return 0.0f;
+}
+
+/* data.h:28-62: float products accumulated in double; cosine keeps the two
+ * squared norms in float and divides by both (x = base row, q = query). */
+double orc_cpu_distance(int metric, int dim, const float *x, const float *q) {
+  double ret = 0.0;
+  if (metric == ORC_L2) {
+    for (int i = 0; i < dim; ++i) {
+      float diff = x[i] - q[i];
+      float sq = diff * diff;
+      ret += (double)sq;
+    }
+    return ret;
+  }
+  if (metric == ORC_IP) {
+    for (int i = 0; i < dim; ++i) {
+      float p = x[i] * q[i];
+      ret -= (double)p;
+    }
+    return ret;
+  }
+  float lena = 0.0f, lenv = 0.0f;
+  for (int i = 0; i < dim; ++i) {
+    float p = x[i] * q[i];
+    ret += (double)p;
+    float pa = x[i] * x[i];
+    lena = lena + pa;
+    float pv = q[i] * q[i];
+    lenv = lenv + pv;
+  }
+  int sign = ret < 0 ? 1 : -1;
+  return (double)sign * (ret * ret / (double)lena / (double)lenv);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Visited hash: fixhash.h:3-109 with __ENABLE_VISITED_DEL                   */
+/* ------------------------------------------------------------------------- */
+
+#define FH_EMPTY (-1)
+#define FH_DELETION (-2)
+static const uint64_t FH_R0 = 0x4bcb391f924ed183ULL; /* fixhash.h:9, first multiplier */
+static const uint64_t FH_R1 = 0xa0ab69ccd854fc0aULL; /* fixhash.h:9, first xor mask   */
+
+/* hash(0, x) = (x ^ (x >> 16) * r0 ^ r1) % cap on 64-bit x, returned as short
+ * (fixhash.h:20-24).  cap <= 32767 keeps the short cast exact. */
+int orc_fixhash_hash(int cap, uint64_t x) {
+  uint64_t v = x ^ ((x >> 16) * FH_R0) ^ FH_R1;
+  return (int)(short)(v % (uint64_t)cap);
+}
+
+static inline int fh_home(int cap, int32_t x) {
+  /* The table stores int; hash() receives it widened to idx_t (size_t). */
+  return orc_fixhash_hash(cap, (uint64_t)(int64_t)x);
+}
+
+void orc_fixhash_init(int32_t *tab, int cap) {
+  for (int i = 0; i < cap; ++i) tab[i] = FH_EMPTY;
+}
+
+/* fixhash.h:38-47: first EMPTY (or DELETION) slot on the probe sequence. */
+void orc_fixhash_add(int32_t *tab, int cap, int32_t x) {
+  int code = fh_home(cap, x);
+  while (tab[code] != FH_EMPTY && tab[code] != FH_DELETION) code = (code + 1) % cap;
+  tab[code] = x;
+}
+
+/* fixhash.h:49-57 */
+int orc_fixhash_test(const int32_t *tab, int cap, int32_t x) {
+  int code = fh_home(cap, x);
+  while (tab[code] != FH_EMPTY) {
+    if (tab[code] == x) return 1;
+    code = (code + 1) % cap;
+  }
+  return 0;
+}
+
+/* fixhash.h:59-93: find x, then walk the run after it and pull entries back
+ * into the hole under the reference's three position cases.  The cases test
+ * the home of the entry that was moved last ("code"), not the hole, which is
+ * why the table can lose an entry (a false negative in later tests); this
+ * restatement keeps that behaviour. */
+void orc_fixhash_del(int32_t *tab, int cap, int32_t x) {
+  int code = fh_home(cap, x);
+  int remove_idx = code;
+  while (tab[remove_idx] != FH_EMPTY) {
+    if (tab[remove_idx] == x) break;
+    remove_idx = (remove_idx + 1) % cap;
+  }
+  if (tab[remove_idx] == FH_EMPTY) return;
+  int next_idx = (remove_idx + 1) % cap;
+  while (tab[next_idx] != FH_EMPTY) {
+    int new_code = fh_home(cap, tab[next_idx]);
+    int cond1 = code <= remove_idx;
+    int cond2 = remove_idx < next_idx;
+    int move;
+    if (cond1 && cond2) move = new_code <= remove_idx;
+    else if (cond1) move = next_idx < new_code && new_code <= remove_idx;
+    else move = next_idx < new_code || new_code <= remove_idx;
+    if (move) {
+      tab[remove_idx] = tab[next_idx];
+      remove_idx = next_idx;
+      code = new_code;
+    }
+    next_idx = (next_idx + 1) % cap;
+  }
+  tab[remove_idx] = FH_EMPTY;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Reference queues: SMMH (smmh2.h) and binary max-heap (bin_heap.h)          */
+/* Elements compare on the distance only (KernelPair, astar_accelerator.h).   */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  double d;
+  uint64_t id;
+} kp_t;
+
+static inline void kp_swap(kp_t *a, kp_t *b) {
+  kp_t c = *a;
+  *a = *b;
+  *b = c;
+}
+
+/* smmh2.h:11-31 */
+static int smmh_adjust_sibling(kp_t *h, int y, int hs) {
+  if (y & 1) {
+    int s = y + 1;
+    if (s >= hs) return y;
+    if (h[y].d > h[s].d) {
+      kp_swap(&h[y], &h[s]);
+      return s;
+    }
+  } else {
+    int s = y - 1;
+    if (h[y].d < h[s].d) {
+      kp_swap(&h[y], &h[s]);
+      return s;
+    }
+  }
+  return y;
+}
+
+/* smmh2.h:58-73 */
+static int smmh_adjust_grandparent(kp_t *h, int y) {
+  if (y <= 2) return y;
+  int g = (y - 3) >> 2;
+  int gl = (g << 1) + 1, gr = (g << 1) + 2;
+  if (h[gl].d > h[y].d) {
+    kp_swap(&h[gl], &h[y]);
+    return gl;
+  } else if (h[gr].d < h[y].d) {
+    kp_swap(&h[gr], &h[y]);
+    return gr;
+  }
+  return y;
+}
+
+/* smmh2.h:75-88: slot 0 is unused, hs = live elements + 1 */
+static void smmh_insert(kp_t *h, int *hs, kp_t e) {
+  int y = *hs;
+  h[(*hs)++] = e;
+  for (;;) {
+    y = smmh_adjust_sibling(h, y, *hs);
+    int x = smmh_adjust_grandparent(h, y);
+    if (x == y) break;
+    y = x;
+  }
+}
+
+/* smmh2.h:90-117 */
+static int smmh_adjust_grandchild(kp_t *h, int y, int hs) {
+  if (y & 1) {
+    if ((y << 1) + 1 >= hs) return y;
+    int cl = (y << 1) + 1, cr = ((y + 1) << 1) + 1;
+    int c = cl;
+    if (cr < hs && h[cr].d < h[cl].d) c = cr;
+    if (h[c].d < h[y].d) {
+      kp_swap(&h[c], &h[y]);
+      return c;
+    }
+  } else {
+    int cl = ((y - 1) << 1) + 2, cr = (y << 1) + 2;
+    if (cl >= hs) return y;
+    int c = cl;
+    if (cr < hs && h[cr].d > h[cl].d) c = cr;
+    if (h[c].d > h[y].d) {
+      kp_swap(&h[c], &h[y]);
+      return c;
+    }
+  }
+  return y;
+}
+
+/* smmh2.h:119-131 (the sibling step's result is not used, as there) */
+static void smmh_deletion(kp_t *h, int idx, int *hs) {
+  h[idx] = h[--(*hs)];
+  int y = idx;
+  for (;;) {
+    smmh_adjust_sibling(h, y, *hs);
+    int x = smmh_adjust_grandchild(h, y, *hs);
+    if (x == y) break;
+    y = x;
+  }
+}
+
+static kp_t smmh_pop_min(kp_t *h, int *hs) {
+  kp_t r = h[1];
+  smmh_deletion(h, 1, hs);
+  return r;
+}
+
+static kp_t smmh_pop_max(kp_t *h, int *hs) {
+  kp_t r = h[2];
+  smmh_deletion(h, 2, hs);
+  return r;
+}
+
+/* bin_heap.h:4-20 (C division truncates, so the root compares with itself) */
+static void bh_push(kp_t *b, int len) {
+  int now = len - 1;
+  int parent = (now - 1) / 2;
+  while (parent >= 0) {
+    if (b[parent].d < b[now].d) {
+      kp_swap(&b[parent], &b[now]);
+      now = parent;
+      parent = (parent - 1) / 2;
+    } else {
+      break;
+    }
+  }
+}
+
+/* bin_heap.h:21-47: the last slot stays inside the sift range */
+static kp_t bh_pop(kp_t *b, int len) {
+  kp_t ret = b[0];
+  b[0] = b[len - 1];
+  int now = 0;
+  while (now + 1 < len) {
+    int left = now * 2 + 1, right = now * 2 + 2, next = -1;
+    if (right < len) next = b[left].d < b[right].d ? right : left;
+    else if (left < len) next = left;
+    if (next == -1 || !(b[now].d < b[next].d)) break;
+    kp_swap(&b[now], &b[next]);
+    now = next;
+  }
+  return ret;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Sorted queues of the GB300 kernel: key (distance, id), ascending           */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  float d;
+  uint32_t pad;
+  uint64_t id;
+} lk_t;
+
+static inline int lk_less(lk_t a, lk_t b) { return a.d < b.d || (a.d == b.d && a.id < b.id); }
+
+static void lk_insert(lk_t *a, int *n, lk_t e) {
+  int pos = *n;
+  while (pos > 0 && lk_less(e, a[pos - 1])) {
+    a[pos] = a[pos - 1];
+    --pos;
+  }
+  a[pos] = e;
+  ++(*n);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Kernel-semantics search                                                    */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  int pq;
+  int maxdeg;
+  kp_t *q, *t;   /* REF */
+  lk_t *lq, *lt; /* LEX */
+  int32_t *tab;
+  uint64_t *cand;
+  float *cdist;
+  uint64_t *tmp_out;
+} kscratch;
+
+static int kscratch_init(kscratch *s, int pq, int maxdeg) {
+  memset(s, 0, sizeof *s);
+  s->pq = pq;
+  s->maxdeg = maxdeg;
+  s->q = (kp_t *)malloc(sizeof(kp_t) * (size_t)(pq + 3));
+  s->t = (kp_t *)malloc(sizeof(kp_t) * (size_t)(pq + 2));
+  s->lq = (lk_t *)malloc(sizeof(lk_t) * (size_t)(pq + 3));
+  s->lt = (lk_t *)malloc(sizeof(lk_t) * (size_t)(pq + 2));
+  s->tab = (int32_t *)malloc(sizeof(int32_t) * (size_t)8 * (size_t)pq);
+  s->cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(maxdeg + 1));
+  s->cdist = (float *)malloc(sizeof(float) * (size_t)(maxdeg + 1));
+  s->tmp_out = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)pq);
+  return s->q && s->t && s->lq && s->lt && s->tab && s->cand && s->cdist && s->tmp_out ? 0 : -1;
+}
+
+static void kscratch_free(kscratch *s) {
+  free(s->q);
+  free(s->t);
+  free(s->lq);
+  free(s->lt);
+  free(s->tab);
+  free(s->cand);
+  free(s->cdist);
+  free(s->tmp_out);
+}
+
+typedef struct {
+  orc_event *log;
+  int cap;
+  int n;
+} evlog;
+
+static inline void ev(evlog *L, int kind, uint64_t id, float d) {
+  if (!L) return;
+  if (L->n < L->cap) {
+    orc_event *e = &L->log[L->n];
+    e->kind = kind;
+    e->pad = 0;
+    e->id = id;
+    e->dist = d;
+    e->pad2 = 0;
+  }
+  L->n++;
+}
+
+static inline const float *row(const orc_index *ix, uint64_t id) {
+  return ix->data + id * (uint64_t)ix->dim;
+}
+
+/* warp_astar_accelerator.h:111-335 for one query (mode REF), or the GB300
+ * kernel's specification of it (mode LEX).  Returns the number of vertices in
+ * the top-pq list at the end. */
+static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, int use_fma,
+                       kscratch *s, uint64_t *out, int32_t *hops_out, int32_t *evals_out,
+                       evlog *L) {
+  const int cap = 8 * pq; /* FixHash<int, TOPK*4*2>, warp_astar_accelerator.h:59-61 */
+  const int shift = ix->shift;
+  int32_t *tab = s->tab;
+  orc_fixhash_init(tab, cap);
+
+  int hs = 1, ts = 0; /* REF: SMMH size (+1 dummy slot) and heap size */
+  int qn = 0;         /* LEX: queue length (ts shared) */
+  int hops = 0, evals = 0;
+
+  float d0 = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, 0), use_fma);
+  evals = 1;
+  if (mode == ORC_MODE_REF) {
+    kp_t e = {(double)d0, 0};
+    smmh_insert(s->q, &hs, e);
+  } else {
+    lk_t e = {d0, 0, 0};
+    lk_insert(s->lq, &qn, e);
+  }
+  orc_fixhash_add(tab, cap, 0);
+
+  for (;;) {
+    uint64_t now_id;
+    float now_d;
+    if (mode == ORC_MODE_REF) {
+      if (hs <= 1) break;
+      kp_t now = smmh_pop_min(s->q, &hs);
+      now_id = now.id;
+      now_d = (float)now.d;
+    } else {
+      if (qn <= 0) break;
+      lk_t now = s->lq[0];
+      memmove(s->lq, s->lq + 1, sizeof(lk_t) * (size_t)(qn - 1));
+      --qn;
+      now_id = now.id;
+      now_d = now.d;
+    }
+    ev(L, ORC_EV_POP, now_id, now_d);
+    orc_fixhash_del(tab, cap, (int32_t)now_id);
+    /* :191 finish test uses <= */
+    float tmax = mode == ORC_MODE_REF ? (ts > 0 ? (float)s->t[0].d : 0.0f)
+                                      : (ts > 0 ? s->lt[ts - 1].d : 0.0f);
+    if (ts == pq && tmax <= now_d) {
+      ev(L, ORC_EV_FINISH, now_id, now_d);
+      break;
+    }
+    ++hops;
+    /* :198-210 */
+    if (mode == ORC_MODE_REF) {
+      kp_t e = {(double)now_d, now_id};
+      s->t[ts++] = e;
+      bh_push(s->t, ts);
+      orc_fixhash_add(tab, cap, (int32_t)now_id);
+      if (ts > pq) {
+        kp_t top = s->t[0];
+        orc_fixhash_del(tab, cap, (int32_t)top.id);
+        bh_pop(s->t, ts);
+        --ts;
+        ev(L, ORC_EV_TEVICT, top.id, (float)top.d);
+      }
+    } else {
+      lk_t e = {now_d, 0, now_id};
+      lk_insert(s->lt, &ts, e);
+      orc_fixhash_add(tab, cap, (int32_t)now_id);
+      if (ts > pq) {
+        lk_t top = s->lt[ts - 1];
+        orc_fixhash_del(tab, cap, (int32_t)top.id);
+        --ts;
+        ev(L, ORC_EV_TEVICT, top.id, top.d);
+      }
+    }
+    /* :211-224 neighbour filter, row order */
+    const uint64_t *grow = ix->graph + (now_id << shift);
+    int degree = (int)grow[0];
+    int m = 0;
+    for (int i = 1; i <= degree; ++i) {
+      uint64_t nb = grow[i];
+      if (orc_fixhash_test(tab, cap, (int32_t)nb)) continue;
+      s->cand[m++] = nb;
+    }
+    /* :237-287 distances */
+    for (int i = 0; i < m; ++i) {
+      s->cdist[i] = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, s->cand[i]), use_fma);
+      ev(L, ORC_EV_TEST, s->cand[i], s->cdist[i]);
+    }
+    evals += m;
+    /* :297-322 select-insert, candidate order */
+    for (int i = 0; i < m; ++i) {
+      float d = s->cdist[i];
+      uint64_t id = s->cand[i];
+      if (mode == ORC_MODE_REF) {
+        if (hs >= pq + 1 && (float)s->q[2].d < d) {
+          ev(L, ORC_EV_SKIP, id, d);
+          continue;
+        }
+        kp_t e = {(double)d, id};
+        smmh_insert(s->q, &hs, e);
+        orc_fixhash_add(tab, cap, (int32_t)id);
+        ev(L, ORC_EV_INSERT, id, d);
+        if (hs >= pq + 2) {
+          kp_t mx = s->q[2];
+          orc_fixhash_del(tab, cap, (int32_t)mx.id);
+          smmh_pop_max(s->q, &hs);
+          ev(L, ORC_EV_QEVICT, mx.id, (float)mx.d);
+        }
+      } else {
+        if (qn >= pq && s->lq[qn - 1].d < d) {
+          ev(L, ORC_EV_SKIP, id, d);
+          continue;
+        }
+        lk_t e = {d, 0, id};
+        lk_insert(s->lq, &qn, e);
+        orc_fixhash_add(tab, cap, (int32_t)id);
+        ev(L, ORC_EV_INSERT, id, d);
+        if (qn >= pq + 1) {
+          lk_t mx = s->lq[qn - 1];
+          orc_fixhash_del(tab, cap, (int32_t)mx.id);
+          --qn;
+          ev(L, ORC_EV_QEVICT, mx.id, mx.d);
+        }
+      }
+    }
+  }
+
+  /* :331-335 output, ascending.  With fewer than pq popped vertices the
+   * reference reads before its heap array (undefined); both modes put the
+   * popped vertices first and ORC_NO_ID after. */
+  for (int i = 0; i < pq; ++i) out[i] = ORC_NO_ID;
+  if (mode == ORC_MODE_REF) {
+    int filled = ts;
+    for (int i = 0; i < filled; ++i) {
+      kp_t e = bh_pop(s->t, filled - i);
+      s->tmp_out[filled - 1 - i] = e.id;
+      s->cdist[0] = (float)e.d; /* scratch, unused */
+    }
+    /* Re-derive distances for the log from the output order. */
+    for (int i = 0; i < filled; ++i) {
+      out[i] = s->tmp_out[i];
+      if (L) ev(L, ORC_EV_OUT, out[i], orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, out[i]), use_fma));
+    }
+  } else {
+    for (int i = 0; i < ts; ++i) {
+      out[i] = s->lt[i].id;
+      ev(L, ORC_EV_OUT, s->lt[i].id, s->lt[i].d);
+    }
+  }
+  if (hops_out) *hops_out = hops;
+  if (evals_out) *evals_out = evals;
+  return ts;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Thread pool helper                                                         */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  const orc_index *ix;
+  const float *queries;
+  int nq, pq, mode, use_fma;
+  uint64_t *out;
+  int32_t *hops, *evals, *popped;
+  volatile int next;
+  volatile int err;
+  int k;
+  int32_t *explored;
+} job_t;
+
+static int maxdeg_of(const orc_index *ix) { return (1 << ix->shift) - 1; }
+
+static void *kworker(void *arg) {
+  job_t *j = (job_t *)arg;
+  kscratch s;
+  if (kscratch_init(&s, j->pq, maxdeg_of(j->ix)) != 0) {
+    j->err = 1;
+    kscratch_free(&s);
+    return NULL;
+  }
+  for (;;) {
+    int i = __sync_fetch_and_add(&j->next, 1);
+    if (i >= j->nq) break;
+    int32_t h = 0, e = 0;
+    int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim, j->pq, j->mode,
+                         j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL);
+    if (j->hops) j->hops[i] = h;
+    if (j->evals) j->evals[i] = e;
+    if (j->popped) j->popped[i] = ts;
+  }
+  kscratch_free(&s);
+  return NULL;
+}
+
+static int check_index(const orc_index *ix) {
+  if (!ix || !ix->data || !ix->graph || ix->n == 0 || ix->dim <= 0) return -1;
+  if (ix->shift < 1 || ix->shift > 12) return -1;
+  if (ix->metric < ORC_L2 || ix->metric > ORC_COS) return -1;
+  return 0;
+}
+
+static int run_pool(void *(*fn)(void *), job_t *j, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  int started = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    if (pthread_create(&th[t], NULL, fn, j) != 0) break;
+    ++started;
+  }
+  if (started == 0) fn(j);
+  for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+  return j->err ? -1 : 0;
+}
+
+int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq, int mode,
+                      int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
+                      int32_t *popped, int nthreads) {
+  if (check_index(ix) || !queries || !out || nq < 0 || pq < 2 || pq > 4095) return -1;
+  if (mode != ORC_MODE_REF && mode != ORC_MODE_LEX) return -1;
+  job_t j;
+  memset(&j, 0, sizeof j);
+  j.ix = ix;
+  j.queries = queries;
+  j.nq = nq;
+  j.pq = pq;
+  j.mode = mode;
+  j.use_fma = use_fma;
+  j.out = out;
+  j.hops = hops;
+  j.evals = evals;
+  j.popped = popped;
+  return run_pool(kworker, &j, nthreads);
+}
+
+int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int mode, int use_fma,
+                          uint64_t *out, orc_event *log, int cap, int *n_events) {
+  if (check_index(ix) || !query || !out || pq < 2 || pq > 4095) return -1;
+  kscratch s;
+  if (kscratch_init(&s, pq, maxdeg_of(ix)) != 0) {
+    kscratch_free(&s);
+    return -1;
+  }
+  evlog L = {log, cap, 0};
+  ksearch_one(ix, query, pq, mode, use_fma, &s, out, NULL, NULL, &L);
+  if (n_events) *n_events = L.n;
+  kscratch_free(&s);
+  return 0;
+}
+
+int orc_classify(const orc_event *a, int na, const orc_event *b, int nb, int *at) {
+  int n = na < nb ? na : nb;
+  for (int i = 0; i < n; ++i) {
+    int same = a[i].kind == b[i].kind && a[i].id == b[i].id && a[i].dist == b[i].dist;
+    if (same) continue;
+    if (at) *at = i;
+    if (a[i].kind == b[i].kind && a[i].dist == b[i].dist && a[i].id != b[i].id) return 1;
+    return 2;
+  }
+  if (na != nb) {
+    if (at) *at = n;
+    return 2;
+  }
+  if (at) *at = -1;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* CPU best-first search, graph.h:169-216                                     */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  double d;
+  uint64_t id;
+} pr_t;
+
+/* std::pair ordering: distance, then id. */
+static inline int pr_less(pr_t a, pr_t b) { return a.d < b.d || (a.d == b.d && a.id < b.id); }
+
+/* Binary heaps; 'minh' keeps the smallest pair on top, 'maxh' the largest. */
+static void heap_push(pr_t *h, int *n, pr_t e, int ismax) {
+  int i = (*n)++;
+  h[i] = e;
+  while (i > 0) {
+    int p = (i - 1) >> 1;
+    int up = ismax ? pr_less(h[p], h[i]) : pr_less(h[i], h[p]);
+    if (!up) break;
+    pr_t t = h[p];
+    h[p] = h[i];
+    h[i] = t;
+    i = p;
+  }
+}
+
+static pr_t heap_pop(pr_t *h, int *n, int ismax) {
+  pr_t top = h[0];
+  h[0] = h[--(*n)];
+  int i = 0;
+  for (;;) {
+    int l = 2 * i + 1, r = l + 1, best = i;
+    if (l < *n && (ismax ? pr_less(h[best], h[l]) : pr_less(h[l], h[best]))) best = l;
+    if (r < *n && (ismax ? pr_less(h[best], h[r]) : pr_less(h[r], h[best]))) best = r;
+    if (best == i) break;
+    pr_t t = h[best];
+    h[best] = h[i];
+    h[i] = t;
+    i = best;
+  }
+  return top;
+}
+
+typedef struct {
+  pr_t *q;
+  int qcap;
+  pr_t *t;
+  uint8_t *visited; /* one byte per vertex, cleared through 'touched' */
+  uint64_t *touched;
+  size_t ntouched, tcap;
+} cscratch;
+
+static int grow_q(cscratch *s, int need) {
+  if (need <= s->qcap) return 0;
+  int nc = s->qcap ? s->qcap : 1024;
+  while (nc < need) nc *= 2;
+  pr_t *nq = (pr_t *)realloc(s->q, sizeof(pr_t) * (size_t)nc);
+  if (!nq) return -1;
+  s->q = nq;
+  s->qcap = nc;
+  return 0;
+}
+
+static int touch(cscratch *s, uint64_t id) {
+  if (s->ntouched == s->tcap) {
+    size_t nc = s->tcap ? s->tcap * 2 : 4096;
+    uint64_t *nt = (uint64_t *)realloc(s->touched, sizeof(uint64_t) * nc);
+    if (!nt) return -1;
+    s->touched = nt;
+    s->tcap = nc;
+  }
+  s->touched[s->ntouched++] = id;
+  s->visited[id] = 1;
+  return 0;
+}
+
+static int csearch_one(const orc_index *ix, const float *qv, int k, cscratch *s, uint64_t *out,
+                       int32_t *explored) {
+  int qn = 0, tn = 0;
+  const int shift = ix->shift;
+  s->ntouched = 0;
+  if (ix->n > 0) {
+    if (touch(s, 0)) return -1;
+    if (grow_q(s, 1)) return -1;
+    pr_t e = {orc_cpu_distance(ix->metric, ix->dim, row(ix, 0), qv), 0};
+    heap_push(s->q, &qn, e, 0);
+  }
+  int explore = 0;
+  for (int iter = 0; iter < 1000000 && qn > 0; ++iter) {
+    pr_t now = s->q[0];
+    if (tn == k && s->t[0].d < now.d) break; /* graph.h:188 uses < */
+    ++explore;
+    heap_pop(s->q, &qn, 0);
+    heap_push(s->t, &tn, now, 1);
+    if (tn > k) heap_pop(s->t, &tn, 1);
+    const uint64_t *grow = ix->graph + (now.id << shift);
+    uint64_t degree = grow[0];
+    for (uint64_t i = 0; i < degree; ++i) {
+      uint64_t nb = grow[i + 1];
+      if (s->visited[nb]) continue;
+      if (grow_q(s, qn + 1)) return -1;
+      pr_t e = {orc_cpu_distance(ix->metric, ix->dim, row(ix, nb), qv), nb};
+      heap_push(s->q, &qn, e, 0);
+      if (touch(s, nb)) return -1;
+    }
+  }
+  for (int i = 0; i < k; ++i) out[i] = ORC_NO_ID;
+  int len = tn;
+  for (int i = len - 1; i >= 0; --i) out[i] = heap_pop(s->t, &tn, 1).id;
+  for (size_t i = 0; i < s->ntouched; ++i) s->visited[s->touched[i]] = 0;
+  if (explored) *explored = explore;
+  return 0;
+}
+
+static void *cworker(void *arg) {
+  job_t *j = (job_t *)arg;
+  cscratch s;
+  memset(&s, 0, sizeof s);
+  s.t = (pr_t *)malloc(sizeof(pr_t) * (size_t)(j->k + 2));
+  s.visited = (uint8_t *)calloc((size_t)j->ix->n, 1);
+  if (!s.t || !s.visited) {
+    j->err = 1;
+  } else {
+    for (;;) {
+      int i = __sync_fetch_and_add(&j->next, 1);
+      if (i >= j->nq) break;
+      int32_t ex = 0;
+      if (csearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim, j->k, &s,
+                      j->out + (size_t)i * (size_t)j->k, &ex)) {
+        j->err = 1;
+        break;
+      }
+      if (j->explored) j->explored[i] = ex;
+    }
+  }
+  free(s.q);
+  free(s.t);
+  free(s.visited);
+  free(s.touched);
+  return NULL;
+}
+
+int orc_cpu_search(const orc_index *ix, const float *queries, int nq, int k, uint64_t *out,
+                   int32_t *explored, int nthreads) {
+  if (check_index(ix) || !queries || !out || nq < 0 || k < 1) return -1;
+  job_t j;
+  memset(&j, 0, sizeof j);
+  j.ix = ix;
+  j.queries = queries;
+  j.nq = nq;
+  j.k = k;
+  j.out = out;
+  j.explored = explored;
+  return run_pool(cworker, &j, nthreads);
+}

@@ -1,0 +1,123 @@
+/*
+ * song_oracle.h -- CPU oracle for the batched best-first graph search.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product (song_gb300/, include/)
+ * links, imports or calls this code; only tests/, __graft_entry__.smoke() and
+ * the cpu_baseline / reference legs of bench.py do, and only as the checker or
+ * the timed CPU baseline.
+ *
+ * It restates, in plain C, three algorithms of sunbelbd/song:
+ *
+ *  1. the warp search kernel  (warp_astar_accelerator.h:41-341), with its
+ *     symmetric min-max candidate queue (smmh2.h:3-164), its top-pq binary
+ *     max-heap (bin_heap.h:3-47) and its open-addressing visited hash with
+ *     backward-shift delete (fixhash.h:3-109, default build flags
+ *     -D__ENABLE_FIXHASH -D__ENABLE_VISITED_DEL, Makefile:21).
+ *     Mode ORC_MODE_REF keeps the reference's heap structures, so the order
+ *     in which equal distances leave the queues is the reference's own.
+ *     Mode ORC_MODE_LEX is the GB300 kernel's specification: the same search,
+ *     the same visited-hash operation sequence, but the queues are kept sorted
+ *     by the key (distance, id), so equal distances leave in id order.  The two
+ *     modes agree on every query in which no decision compares two different
+ *     ids at the same distance; orc_classify() finds the first decision at
+ *     which they part and says whether it is such a tie.
+ *
+ *  2. the CPU best-first search (graph.h:169-216) that the reference's graph
+ *     builder runs and that song.cpu times: unbounded queue, permanent visited
+ *     set, std::pair ordering (distance, id).
+ *
+ *  3. the distance arithmetic of each: the kernel's lane-strided FP32 sums
+ *     with the xor butterfly (warp_astar_accelerator.h:115-163, :237-287) and
+ *     the CPU's float products accumulated in double (data.h:28-62).
+ *
+ * Parity with the reference is pinned by tests/golden/ fixtures produced by
+ * the reference's own containers and CPU code (oracle/ref_harness.cpp).
+ */
+#ifndef SONG_ORACLE_H
+#define SONG_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_L2 = 0, ORC_IP = 1, ORC_COS = 2 };      /* KernelFixedDegreeGraph<0|1|2> */
+enum { ORC_MODE_REF = 0, ORC_MODE_LEX = 1 };
+
+/* Output slot that the search did not fill (fewer than pq vertices popped). */
+#define ORC_NO_ID UINT64_MAX
+
+/* Event kinds of the per-query decision log used by orc_classify(). */
+enum {
+  ORC_EV_POP = 1,     /* candidate queue minimum removed            */
+  ORC_EV_FINISH = 2,  /* search stopped on the popped vertex          */
+  ORC_EV_TEVICT = 3,  /* top-pq maximum dropped                       */
+  ORC_EV_SKIP = 4,    /* candidate rejected by the select-insert test */
+  ORC_EV_INSERT = 5,  /* candidate inserted                           */
+  ORC_EV_QEVICT = 6,  /* candidate queue maximum dropped              */
+  ORC_EV_TEST = 7,    /* neighbour passed the visited test            */
+  ORC_EV_OUT = 8      /* one output slot, ascending                   */
+};
+
+typedef struct {
+  int32_t kind;
+  uint32_t pad;
+  uint64_t id;
+  float dist;
+  uint32_t pad2;
+} orc_event;
+
+/* Index view: bfsg.data (n x dim float32) and bfsg.graph (n << shift uint64,
+ * slot 0 = out-degree, then zero-based neighbour ids). */
+typedef struct {
+  const float *data;
+  const uint64_t *graph;
+  uint64_t n;
+  int32_t dim;
+  int32_t shift;
+  int32_t metric;
+  int32_t pad;
+} orc_index;
+
+/* Kernel distance of one base row x to query q: lane l of a 32-wide warp sums
+ * dims l, l+32, ... with fused multiply-add (use_fma=1, nvcc's default
+ * contraction) or separate multiply and add (use_fma=0); partial sums are
+ * combined by the xor butterfly 16,8,4,2,1. */
+float orc_kernel_distance(int metric, int dim, const float *q, const float *x, int use_fma);
+
+/* CPU distance of data.h:28-62 (x = base row, q = query). */
+double orc_cpu_distance(int metric, int dim, const float *x, const float *q);
+
+/* Batched kernel-semantics search.  out: nq x pq ids (ascending distance);
+ * hops/evals/popped may be NULL.  Returns 0, or -1 on bad arguments. */
+int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq, int mode,
+                      int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
+                      int32_t *popped, int nthreads);
+
+/* One query with its decision log (at most cap events; *n_events gets the
+ * number produced, which may exceed cap). */
+int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int mode, int use_fma,
+                          uint64_t *out, orc_event *log, int cap, int *n_events);
+
+/* Compare the REF and LEX logs of one query.  Returns 0 if identical, 1 if the
+ * first difference is a tie (same event kind, same distance, different id),
+ * 2 if it is anything else.  *at gets the index of the first difference. */
+int orc_classify(const orc_event *a, int na, const orc_event *b, int nb, int *at);
+
+/* CPU best-first search of graph.h:169-216 with result size k.  out: nq x k
+ * (ORC_NO_ID past the result length); explored may be NULL. */
+int orc_cpu_search(const orc_index *ix, const float *queries, int nq, int k, uint64_t *out,
+                   int32_t *explored, int nthreads);
+
+/* The visited hash on its own, for unit tests: a table of 8*pq int32 slots. */
+int orc_fixhash_hash(int cap, uint64_t x);
+void orc_fixhash_init(int32_t *tab, int cap);
+void orc_fixhash_add(int32_t *tab, int cap, int32_t x);
+int orc_fixhash_test(const int32_t *tab, int cap, int32_t x);
+void orc_fixhash_del(int32_t *tab, int cap, int32_t x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

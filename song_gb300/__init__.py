@@ -1,0 +1,226 @@
+"""song_gb300: batched best-first graph search on GB300 (sm_103a).
+
+Python view of the C ABI in include/song_gb300.h (libsong_gb300.so, built
+in-tree by song_gb300/build.py).  The search runs only in the CUDA kernels of
+that library; there is no CPU path, and importing this package fails if the
+library has not been built.
+
+Reference surface mirrored here (sunbelbd/song):
+  * Index.search          <- GraphWrapper::search_top_k_batch (kernelgraph.h:269-272)
+  * astar_search_batch    <- WarpAStarAccelerator::astar_multi_start_search_batch
+                             (warp_astar_accelerator.h:347-423)
+  * graph_build           <- FixedDegreeGraph::add_vertex loop (graph.h:149-167, main.cu:15-18)
+  * read/write bfsg files <- Data::dump/load, *Graph::dump/load (data.h:164-175, kernelgraph.h:255-267)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB_PATH
+
+SONG_OK, SONG_ERR_ARG, SONG_ERR_OOM, SONG_ERR_TIMEOUT, SONG_ERR_CUDA, SONG_ERR_IO = range(6)
+METRICS = {"l2": 0, "ip": 1, "cos": 2}
+STORAGES = {"f32": 0, "bf16": 1, "fp8": 2}
+MAX_PQ = 1023
+NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+# Every function include/song_gb300.h declares; tests check the library exports them.
+EXPORTED = [
+    "song_status_string", "song_last_error", "song_index_create", "song_index_load",
+    "song_index_free", "song_index_info", "song_search", "song_search_device",
+    "song_astar_search_batch", "song_graph_build", "song_debug_fixhash",
+]
+
+
+class SongError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (status %d): %s" % (_STATUS.get(status, "error"), status, message))
+        self.status = status
+
+
+_STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "device wait timed out",
+           4: "CUDA error", 5: "I/O error"}
+
+_lib = None
+
+
+def load_library():
+    """Load libsong_gb300.so; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libsong_gb300.so not built: run `python -c \"import __graft_entry__ as g; "
+                          "g.build()\"` or `python song_gb300/build.py`")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    i32 = ctypes.c_int
+    u64 = ctypes.c_uint64
+    L.song_status_string.restype = ctypes.c_char_p
+    L.song_status_string.argtypes = [i32]
+    L.song_last_error.restype = ctypes.c_char_p
+    L.song_last_error.argtypes = []
+    L.song_index_create.restype = i32
+    L.song_index_create.argtypes = [P, P, u64, i32, i32, i32, i32, i32, ctypes.POINTER(P)]
+    L.song_index_load.restype = i32
+    L.song_index_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, u64, i32, i32, i32, i32, i32,
+                                  ctypes.POINTER(P)]
+    L.song_index_free.restype = i32
+    L.song_index_free.argtypes = [P]
+    L.song_index_info.restype = i32
+    L.song_index_info.argtypes = [P, P, P, P, P, P, P]
+    L.song_search.restype = i32
+    L.song_search.argtypes = [P, P, i32, i32, i32, P, P, P]
+    L.song_search_device.restype = i32
+    L.song_search_device.argtypes = [P, P, i32, i32, i32, P, P, P, P]
+    L.song_astar_search_batch.restype = i32
+    L.song_astar_search_batch.argtypes = [P, i32, i32, P, P, P, i32, u64, i32, i32]
+    L.song_graph_build.restype = i32
+    L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
+    L.song_debug_fixhash.restype = i32
+    L.song_debug_fixhash.argtypes = [P, i32, i32, P]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != SONG_OK:
+        msg = load_library().song_last_error().decode(errors="replace")
+        raise SongError(rc, msg)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _metric(m):
+    return METRICS[m] if isinstance(m, str) else int(m)
+
+
+def _storage(s):
+    return STORAGES[s] if isinstance(s, str) else int(s)
+
+
+class Index:
+    """A resident index on one GPU (song_index_create / song_index_load)."""
+
+    def __init__(self, graph, data, shift, metric, storage="f32", device=0, _handle=None):
+        L = load_library()
+        self._h = ctypes.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            data = np.ascontiguousarray(data, dtype=np.float32)
+            graph = np.ascontiguousarray(graph, dtype=np.uint64).reshape(-1)
+            n, dim = data.shape
+            if graph.size != (n << shift):
+                raise ValueError("graph has %d slots, expected n << shift = %d" % (graph.size, n << shift))
+            _check(L.song_index_create(_ptr(graph), _ptr(data), n, dim, shift, _metric(metric),
+                                       _storage(storage), device, ctypes.byref(self._h)))
+        n = ctypes.c_uint64()
+        dim, sh, me, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        nb = ctypes.c_uint64()
+        _check(L.song_index_info(self._h, ctypes.byref(n), ctypes.byref(dim), ctypes.byref(sh),
+                                 ctypes.byref(me), ctypes.byref(st), ctypes.byref(nb)))
+        self.n, self.dim, self.shift, self.metric, self.storage = n.value, dim.value, sh.value, me.value, st.value
+        self.device = device
+
+    @classmethod
+    def load(cls, graph_path, data_path, n, dim, shift, metric, storage="f32", device=0):
+        L = load_library()
+        h = ctypes.c_void_p()
+        _check(L.song_index_load(graph_path.encode(), data_path.encode(), n, dim, shift,
+                                 _metric(metric), _storage(storage), device, ctypes.byref(h)))
+        return cls(None, None, shift, metric, storage, device, _handle=h)
+
+    def device_bytes(self):
+        nb = ctypes.c_uint64()
+        _check(load_library().song_index_info(self._h, None, None, None, None, None, ctypes.byref(nb)))
+        return nb.value
+
+    def search(self, queries, pq, k=None, stats=False):
+        """Host-buffer search (song_search): returns nq x k uint64 ids, and
+        per-query hops and distance evaluations when stats=True."""
+        k = pq if k is None else k
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim != 2 or q.shape[1] != self.dim:
+            raise ValueError("queries must be nq x %d" % self.dim)
+        nq = q.shape[0]
+        out = np.empty((nq, k), dtype=np.uint64)
+        hops = np.empty(nq, dtype=np.int32) if stats else None
+        evals = np.empty(nq, dtype=np.int32) if stats else None
+        _check(load_library().song_search(self._h, _ptr(q), nq, pq, k, _ptr(out), _ptr(hops), _ptr(evals)))
+        return (out, hops, evals) if stats else out
+
+    def search_device(self, q_ptr, nq, pq, k, out_ptr, hops_ptr=None, evals_ptr=None, stream=None):
+        """Device-buffer search (song_search_device): raw device pointers
+        (e.g. torch.Tensor.data_ptr()), enqueued on `stream` (a raw
+        cudaStream_t handle or None)."""
+        _check(load_library().song_search_device(self._h, ctypes.c_void_p(q_ptr), nq, pq, k,
+                                                 ctypes.c_void_p(out_ptr),
+                                                 ctypes.c_void_p(hops_ptr) if hops_ptr else None,
+                                                 ctypes.c_void_p(evals_ptr) if evals_ptr else None,
+                                                 ctypes.c_void_p(stream) if stream else None))
+
+    def free(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load_library().song_index_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.free()
+
+
+def astar_search_batch(queries, pq, data, graph, shift, metric):
+    """One-shot drop-in for astar_multi_start_search_batch: nq x pq ids."""
+    q = np.ascontiguousarray(queries, dtype=np.float32)
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    graph = np.ascontiguousarray(graph, dtype=np.uint64)
+    n, dim = data.shape
+    out = np.empty((q.shape[0], pq), dtype=np.uint64)
+    _check(load_library().song_astar_search_batch(_ptr(q), q.shape[0], pq, _ptr(out), _ptr(data),
+                                                  _ptr(graph), shift, n, dim, _metric(metric)))
+    return out
+
+
+def graph_build(data, metric, shift=5, search_degree=15, fixed_degree=31, budget=150,
+                batch_div=0, nthreads=None):
+    """Proximity graph in the bfsg.graph layout (n << shift uint64)."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    n, dim = data.shape
+    out = np.empty(n << shift, dtype=np.uint64)
+    _check(load_library().song_graph_build(_ptr(data), n, dim, _metric(metric), shift, search_degree,
+                                           fixed_degree, budget, batch_div,
+                                           nthreads or os.cpu_count() or 1, _ptr(out)))
+    return out
+
+
+def debug_fixhash(ids, pq):
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    out = np.empty(ids.size, dtype=np.int32)
+    _check(load_library().song_debug_fixhash(_ptr(ids), ids.size, pq, _ptr(out)))
+    return out
+
+
+def write_bfsg(graph_path, data_path, graph, data):
+    """bfsg.graph (uint64) and bfsg.data (float32) as the reference dumps them."""
+    np.ascontiguousarray(graph, dtype=np.uint64).tofile(graph_path)
+    np.ascontiguousarray(data, dtype=np.float32).tofile(data_path)
+
+
+def read_bfsg(graph_path, data_path, n, dim, shift):
+    graph = np.fromfile(graph_path, dtype=np.uint64, count=n << shift)
+    data = np.fromfile(data_path, dtype=np.float32, count=n * dim).reshape(n, dim)
+    return graph, data

@@ -1,0 +1,360 @@
+// capi.cu -- the extern "C" boundary (include/song_gb300.h): resident index,
+// search entry points with host or device buffers, and the one-shot form with
+// the reference's argument list.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "song_gb300.h"
+
+struct song_index {
+  int device = 0;
+  song::DeviceIndex dx;
+  void *d_rows = nullptr;
+  uint32_t *d_adj = nullptr;
+  float *d_scale = nullptr;
+  float *d_rows_f32 = nullptr;
+  uint32_t *d_counter = nullptr;
+  int32_t *d_error = nullptr;
+  cudaStream_t stream = nullptr;
+  // device staging for the host-buffer entry point
+  float *d_q = nullptr;
+  size_t cap_q = 0;
+  uint64_t *d_out = nullptr;
+  size_t cap_out = 0;
+  int32_t *d_stats = nullptr;
+  size_t cap_stats = 0;
+  uint64_t device_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define SONG_CUDA(call)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "%s: %s", \
+                  #call, cudaGetErrorString(e_));                                         \
+  } while (0)
+
+// Makes `dev` current for the scope and restores the caller's device.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+template <class T>
+int grow(T **p, size_t *cap, size_t need, uint64_t *acct) {
+  if (need <= *cap) return SONG_OK;
+  if (*p) {
+    cudaFree(*p);
+    *acct -= *cap * sizeof(T);
+  }
+  *p = nullptr;
+  *cap = 0;
+  size_t n = need < 1024 ? 1024 : need;
+  SONG_CUDA(cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T)));
+  *cap = n;
+  *acct += n * sizeof(T);
+  return SONG_OK;
+}
+
+void release(song_index *ix) {
+  if (!ix) return;
+  cudaFree(ix->d_rows);
+  cudaFree(ix->d_adj);
+  cudaFree(ix->d_scale);
+  if (ix->d_rows_f32 && ix->d_rows_f32 != ix->d_rows) cudaFree(ix->d_rows_f32);
+  cudaFree(ix->d_counter);
+  cudaFree(ix->d_error);
+  cudaFree(ix->d_q);
+  cudaFree(ix->d_out);
+  cudaFree(ix->d_stats);
+  if (ix->stream) cudaStreamDestroy(ix->stream);
+  delete ix;
+}
+
+int check_search_args(const song_index *ix, int nq, int pq, int k) {
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (nq < 0) return fail(SONG_ERR_ARG, "nq must be >= 0");
+  if (pq < 2 || pq > SONG_MAX_PQ) return fail(SONG_ERR_ARG, "pq must be in [2, %d]", SONG_MAX_PQ);
+  if (k < 1 || k > pq) return fail(SONG_ERR_ARG, "k must be in [1, pq]");
+  uint32_t wb = song::search_warp_bytes(ix->dx, pq);
+  if (wb * 4u > 227u * 1024u)
+    return fail(SONG_ERR_ARG, "pq %d with dim %d needs %u B of shared memory per warp", pq,
+                ix->dx.dim, wb);
+  return SONG_OK;
+}
+
+int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_out,
+           int32_t *d_hops, int32_t *d_evals, cudaStream_t s) {
+  song::SearchCall c;
+  c.queries = d_q;
+  c.nq = nq;
+  c.pq = pq;
+  c.k = k;
+  c.out = d_out;
+  c.hops = d_hops;
+  c.evals = d_evals;
+  c.counter = ix->d_counter;
+  c.error = ix->d_error;
+  SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
+  int e = song::launch_search(ix->dx, c, s);
+  if (e == -1) return fail(SONG_ERR_ARG, "unsupported search shape");
+  if (e != 0) return fail(SONG_ERR_CUDA, "search launch: %s", cudaGetErrorString((cudaError_t)e));
+  return SONG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *song_status_string(int status) {
+  switch (status) {
+    case SONG_OK: return "ok";
+    case SONG_ERR_ARG: return "invalid argument";
+    case SONG_ERR_OOM: return "out of memory";
+    case SONG_ERR_TIMEOUT: return "device wait timed out";
+    case SONG_ERR_CUDA: return "CUDA error";
+    case SONG_ERR_IO: return "I/O error";
+    default: return "unknown status";
+  }
+}
+
+const char *song_last_error(void) { return g_last_error.c_str(); }
+
+int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int dim, int shift,
+                      int metric, int storage, int device, song_index **out) {
+  g_last_error.clear();
+  if (!out) return fail(SONG_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  if (!graph || !data) return fail(SONG_ERR_ARG, "null graph or data");
+  if (n < 1 || n > 0x7fffffffull) return fail(SONG_ERR_ARG, "n must be in [1, 2^31)");
+  if (dim < 1 || dim > 65536) return fail(SONG_ERR_ARG, "dim must be in [1, 65536]");
+  if (shift < 1 || shift > SONG_MAX_SHIFT)
+    return fail(SONG_ERR_ARG, "shift must be in [1, %d]", SONG_MAX_SHIFT);
+  if (metric < SONG_METRIC_L2 || metric > SONG_METRIC_COS) return fail(SONG_ERR_ARG, "bad metric");
+  if (storage != SONG_STORAGE_F32) return fail(SONG_ERR_ARG, "storage %d not available", storage);
+
+  // The reference reads degree and ids unchecked (warp_astar_accelerator.h:212-214);
+  // a malformed row would make it read out of bounds, so reject it here.
+  const uint64_t slots = n << shift;
+  const uint64_t maxdeg = (1ull << shift) - 1;
+  std::vector<uint32_t> adj(slots, 0u);
+  for (uint64_t v = 0; v < n; ++v) {
+    const uint64_t *row = graph + (v << shift);
+    const uint64_t deg = row[0];
+    if (deg > maxdeg)
+      return fail(SONG_ERR_ARG, "vertex %llu has degree %llu > %llu", (unsigned long long)v,
+                  (unsigned long long)deg, (unsigned long long)maxdeg);
+    uint32_t *arow = adj.data() + (v << shift);
+    arow[0] = static_cast<uint32_t>(deg);
+    for (uint64_t i = 1; i <= deg; ++i) {
+      if (row[i] >= n)
+        return fail(SONG_ERR_ARG, "vertex %llu has neighbour %llu >= n", (unsigned long long)v,
+                    (unsigned long long)row[i]);
+      arow[i] = static_cast<uint32_t>(row[i]);
+    }
+  }
+
+  DeviceGuard g(device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", device);
+  song_index *ix = new song_index();
+  ix->device = device;
+  song::DeviceIndex &dx = ix->dx;
+  dx.n = n;
+  dx.dim = dim;
+  dx.shift = shift;
+  dx.metric = metric;
+  dx.storage = storage;
+  dx.dpad = (dim + 3) / 4 * 4;
+  dx.row_bytes = static_cast<uint32_t>(dx.dpad) * 4u;
+  dx.f32_row_bytes = dx.row_bytes;
+
+  auto bail = [&](int code) {
+    release(ix);
+    return code;
+  };
+  cudaError_t e;
+#define SONG_CUDA_IX(call)                                                                  \
+  do {                                                                                      \
+    e = (call);                                                                             \
+    if (e != cudaSuccess)                                                                   \
+      return bail(fail(e == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "%s: %s", \
+                       #call, cudaGetErrorString(e)));                                      \
+  } while (0)
+  SONG_CUDA_IX(cudaStreamCreateWithFlags(&ix->stream, cudaStreamNonBlocking));
+  const size_t rows_bytes = static_cast<size_t>(n) * dx.row_bytes;
+  SONG_CUDA_IX(cudaMalloc(&ix->d_rows, rows_bytes));
+  ix->device_bytes += rows_bytes;
+  SONG_CUDA_IX(cudaMemsetAsync(ix->d_rows, 0, rows_bytes, ix->stream));
+  SONG_CUDA_IX(cudaMemcpy2DAsync(ix->d_rows, dx.row_bytes, data, sizeof(float) * dim,
+                                 sizeof(float) * dim, n, cudaMemcpyHostToDevice, ix->stream));
+  SONG_CUDA_IX(cudaMalloc(&ix->d_adj, slots * sizeof(uint32_t)));
+  ix->device_bytes += slots * sizeof(uint32_t);
+  SONG_CUDA_IX(cudaMemcpyAsync(ix->d_adj, adj.data(), slots * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice, ix->stream));
+  SONG_CUDA_IX(cudaMalloc(&ix->d_counter, 256));
+  SONG_CUDA_IX(cudaMalloc(&ix->d_error, 256));
+  ix->device_bytes += 512;
+  SONG_CUDA_IX(cudaMemsetAsync(ix->d_error, 0, 256, ix->stream));
+  SONG_CUDA_IX(cudaStreamSynchronize(ix->stream));
+#undef SONG_CUDA_IX
+  dx.rows = ix->d_rows;
+  dx.rows_f32 = static_cast<const float *>(ix->d_rows);
+  dx.adj = ix->d_adj;
+  *out = ix;
+  return SONG_OK;
+}
+
+int song_index_load(const char *graph_path, const char *data_path, uint64_t n, int dim, int shift,
+                    int metric, int storage, int device, song_index **out) {
+  g_last_error.clear();
+  if (!graph_path || !data_path || !out) return fail(SONG_ERR_ARG, "null argument");
+  if (n < 1 || dim < 1 || shift < 1 || shift > SONG_MAX_SHIFT)
+    return fail(SONG_ERR_ARG, "bad n, dim or shift");
+  std::vector<uint64_t> graph(static_cast<size_t>(n) << shift);
+  std::vector<float> data(static_cast<size_t>(n) * dim);
+  FILE *fg = fopen(graph_path, "rb");
+  if (!fg) return fail(SONG_ERR_IO, "cannot open %s", graph_path);
+  size_t got = fread(graph.data(), sizeof(uint64_t), graph.size(), fg);
+  fclose(fg);
+  if (got != graph.size()) return fail(SONG_ERR_IO, "%s: short read", graph_path);
+  FILE *fd = fopen(data_path, "rb");
+  if (!fd) return fail(SONG_ERR_IO, "cannot open %s", data_path);
+  got = fread(data.data(), sizeof(float), data.size(), fd);
+  fclose(fd);
+  if (got != data.size()) return fail(SONG_ERR_IO, "%s: short read", data_path);
+  return song_index_create(graph.data(), data.data(), n, dim, shift, metric, storage, device, out);
+}
+
+int song_index_free(song_index *index) {
+  if (!index) return SONG_OK;
+  DeviceGuard g(index->device);
+  release(index);
+  return SONG_OK;
+}
+
+int song_index_info(const song_index *ix, uint64_t *n, int *dim, int *shift, int *metric,
+                    int *storage, uint64_t *device_bytes) {
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (n) *n = ix->dx.n;
+  if (dim) *dim = ix->dx.dim;
+  if (shift) *shift = ix->dx.shift;
+  if (metric) *metric = ix->dx.metric;
+  if (storage) *storage = ix->dx.storage;
+  if (device_bytes) *device_bytes = ix->device_bytes;
+  return SONG_OK;
+}
+
+int song_search(song_index *ix, const float *queries, int nq, int pq, int k, uint64_t *out,
+                int32_t *hops, int32_t *evals) {
+  g_last_error.clear();
+  int rc = check_search_args(ix, nq, pq, k);
+  if (rc) return rc;
+  if (nq == 0) return SONG_OK;
+  if (!queries || !out) return fail(SONG_ERR_ARG, "null queries or out");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  const size_t qn = static_cast<size_t>(nq) * ix->dx.dim;
+  const size_t on = static_cast<size_t>(nq) * k;
+  if ((rc = grow(&ix->d_q, &ix->cap_q, qn, &ix->device_bytes))) return rc;
+  if ((rc = grow(&ix->d_out, &ix->cap_out, on, &ix->device_bytes))) return rc;
+  const bool stats = hops || evals;
+  if (stats && (rc = grow(&ix->d_stats, &ix->cap_stats, 2 * static_cast<size_t>(nq),
+                          &ix->device_bytes)))
+    return rc;
+  cudaStream_t s = ix->stream;
+  SONG_CUDA(cudaMemcpyAsync(ix->d_q, queries, qn * sizeof(float), cudaMemcpyHostToDevice, s));
+  rc = launch(ix, ix->d_q, nq, pq, k, ix->d_out, stats ? ix->d_stats : nullptr,
+              stats ? ix->d_stats + nq : nullptr, s);
+  if (rc) return rc;
+  SONG_CUDA(cudaMemcpyAsync(out, ix->d_out, on * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if (hops)
+    SONG_CUDA(cudaMemcpyAsync(hops, ix->d_stats, nq * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (evals)
+    SONG_CUDA(cudaMemcpyAsync(evals, ix->d_stats + nq, nq * sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s));
+  int32_t err = 0;
+  SONG_CUDA(cudaMemcpyAsync(&err, ix->d_error, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  SONG_CUDA(cudaStreamSynchronize(s));
+  if (err) return fail(SONG_ERR_TIMEOUT, "a bulk copy wait timed out in the search kernel");
+  return SONG_OK;
+}
+
+int song_search_device(song_index *ix, const float *d_queries, int nq, int pq, int k,
+                       uint64_t *d_out, int32_t *d_hops, int32_t *d_evals, void *stream) {
+  g_last_error.clear();
+  int rc = check_search_args(ix, nq, pq, k);
+  if (rc) return rc;
+  if (nq == 0) return SONG_OK;
+  if (!d_queries || !d_out) return fail(SONG_ERR_ARG, "null queries or out");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  return launch(ix, d_queries, nq, pq, k, d_out, d_hops, d_evals,
+                static_cast<cudaStream_t>(stream));
+}
+
+int song_astar_search_batch(const float *queries, int nq, int pq, uint64_t *results,
+                            const float *h_data, const uint64_t *h_graph, int vertex_offset_shift,
+                            uint64_t num, int dim, int metric) {
+  song_index *ix = nullptr;
+  int rc = song_index_create(h_graph, h_data, num, dim, vertex_offset_shift, metric,
+                             SONG_STORAGE_F32, 0, &ix);
+  if (rc) return rc;
+  rc = song_search(ix, queries, nq, pq, pq, results, nullptr, nullptr);
+  std::string keep = g_last_error;
+  song_index_free(ix);
+  g_last_error = keep;
+  return rc;
+}
+
+int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_out) {
+  g_last_error.clear();
+  if (count < 0 || pq < 2 || pq > SONG_MAX_PQ || (count > 0 && (!ids || !slots_out)))
+    return fail(SONG_ERR_ARG, "bad arguments");
+  if (count == 0) return SONG_OK;
+  uint32_t *d_ids = nullptr;
+  int32_t *d_out = nullptr;
+  SONG_CUDA(cudaMalloc(&d_ids, count * sizeof(uint32_t)));
+  cudaError_t e = cudaMalloc(&d_out, count * sizeof(int32_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d_ids, ids, count * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    int le = song::launch_debug_fixhash(d_ids, count, pq, d_out, 0);
+    e = static_cast<cudaError_t>(le);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpy(slots_out, d_out, count * sizeof(int32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d_ids);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "debug fixhash: %s", cudaGetErrorString(e));
+  return SONG_OK;
+}
+
+}  // extern "C"

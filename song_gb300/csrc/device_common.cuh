@@ -1,0 +1,259 @@
+// device_common.cuh -- warp-cooperative building blocks of the search kernel:
+// bulk-copy / mbarrier wrappers (inline PTX, sm_90+ forms valid on sm_103a),
+// the visited hash and the sorted candidate / top-pq queues, all held in the
+// shared memory slice of one warp.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace song {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int32_t FH_EMPTY = -1;     // fixhash.h:3 EMPTY
+constexpr int32_t FH_DELETION = -2;  // fixhash.h:3 DELETION (never written with backward-shift delete)
+// fixhash.h:9, the first multiplier / xor pair used by hash(0, x).
+constexpr uint64_t FH_R0 = 0x4bcb391f924ed183ULL;
+constexpr uint64_t FH_R1 = 0xa0ab69ccd854fc0aULL;
+
+// Bounded waits: an mbarrier that does not complete within this many polls
+// (each poll may itself suspend in hardware) sets the error flag and returns.
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared, completion counted on `bar` in bytes.
+// dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// Keys of the sorted queues: (distance, id) in one uint64 whose unsigned
+// order is (distance ascending, id ascending).  The distance is mapped to an
+// order-preserving uint32 after -0 is folded onto +0, so that the reference's
+// float comparisons (which treat -0 == +0) and key comparisons agree.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t dist_bits(float d) {
+  if (d == 0.0f) d = 0.0f;
+  uint32_t u = __float_as_uint(d);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ uint64_t make_key(float d, uint32_t id) {
+  return (static_cast<uint64_t>(dist_bits(d)) << 32) | id;
+}
+__device__ __forceinline__ uint32_t key_dist(uint64_t k) { return static_cast<uint32_t>(k >> 32); }
+__device__ __forceinline__ uint32_t key_id(uint64_t k) { return static_cast<uint32_t>(k); }
+
+// ---------------------------------------------------------------------------
+// Visited hash: the reference's FixHash<int, 8*pq> (fixhash.h) in the warp's
+// shared memory, with the same slot function, linear probing and
+// backward-shift delete, so that membership answers (including the rare
+// entries its delete loses) are the reference's.
+// ---------------------------------------------------------------------------
+struct VisitedHash {
+  int32_t *tab;
+  int cap;        // 8 * pq
+  uint64_t magic; // floor((2^64 - 1) / cap): v % cap by one high multiply and one correction
+
+  // hash(0, x) = (x ^ (x >> 16) * r0 ^ r1) % cap (fixhash.h:20-24).  x is the
+  // stored int widened to 64 bits; ids are < 2^31 so that is the id itself.
+  __device__ __forceinline__ int slot(uint32_t id) const {
+    uint64_t x = id;
+    uint64_t v = x ^ ((x >> 16) * FH_R0) ^ FH_R1;
+    uint64_t q = __umul64hi(v, magic);
+    uint64_t r = v - q * static_cast<uint64_t>(cap);
+    if (r >= static_cast<uint64_t>(cap)) r -= static_cast<uint64_t>(cap);
+    return static_cast<int>(r);
+  }
+
+  __device__ __forceinline__ int wrap(int s) const {
+    while (s >= cap) s -= cap;
+    return s;
+  }
+
+  __device__ __forceinline__ void clear(int lane) {
+    for (int i = lane; i < cap; i += 32) tab[i] = FH_EMPTY;
+    __syncwarp();
+  }
+
+  // One lane, own key (fixhash.h:49-57).
+  __device__ __forceinline__ bool test(uint32_t id) const {
+    int c = slot(id);
+    for (int i = 0; i < cap; ++i) {
+      int32_t v = tab[c];
+      if (v == FH_EMPTY) return false;
+      if (v == static_cast<int32_t>(id)) return true;
+      c = c + 1 == cap ? 0 : c + 1;
+    }
+    return false;
+  }
+
+  // Whole warp, one key (fixhash.h:38-47): first EMPTY/DELETION slot on the
+  // probe sequence, found 32 slots at a time with a ballot.
+  __device__ __forceinline__ void add(uint32_t id, int lane) {
+    int base = slot(id);
+    for (int w = 0; w * 32 < cap + 32; ++w) {
+      int s = wrap(base + lane);
+      int32_t v = tab[s];
+      unsigned b = __ballot_sync(FULL, v == FH_EMPTY || v == FH_DELETION);
+      if (b) {
+        if (lane == __ffs(b) - 1) tab[s] = static_cast<int32_t>(id);
+        break;
+      }
+      base = wrap(base + 32);
+    }
+    __syncwarp();
+  }
+
+  // Whole warp, one key (fixhash.h:59-93).  The run after the removed entry is
+  // read 32 slots at a time; the reference's sequential case analysis then
+  // runs uniformly over it, with each lane's slot value and home slot fetched
+  // by shuffle.
+  __device__ __forceinline__ void del(uint32_t id, int lane) {
+    const int32_t x = static_cast<int32_t>(id);
+    int code = slot(id);
+    int r = -1;
+    int base = code;
+    for (int w = 0; w * 32 < cap + 32; ++w) {
+      int s = wrap(base + lane);
+      int32_t v = tab[s];
+      unsigned be = __ballot_sync(FULL, v == FH_EMPTY);
+      unsigned bm = __ballot_sync(FULL, v == x);
+      unsigned before = be ? ((1u << (__ffs(be) - 1)) - 1u) : FULL;
+      unsigned hit = bm & before;
+      if (hit) {
+        r = wrap(base + __ffs(hit) - 1);
+        break;
+      }
+      if (be) return;  // not present
+      base = wrap(base + 32);
+    }
+    if (r < 0) return;
+    int nbase = wrap(r + 1);
+    for (int w = 0; w * 32 < cap + 32; ++w) {
+      int s = wrap(nbase + lane);
+      int32_t v = tab[s];
+      int home = v >= 0 ? slot(static_cast<uint32_t>(v)) : 0;
+      unsigned be = __ballot_sync(FULL, v == FH_EMPTY);
+      int run = be ? __ffs(be) - 1 : 32;
+      for (int i = 0; i < run; ++i) {
+        int nxt = wrap(nbase + i);
+        int ncode = __shfl_sync(FULL, home, i);
+        int32_t val = __shfl_sync(FULL, v, i);
+        bool cond1 = code <= r;
+        bool cond2 = r < nxt;
+        bool move;
+        if (cond1 && cond2) move = ncode <= r;
+        else if (cond1) move = nxt < ncode && ncode <= r;
+        else move = nxt < ncode || ncode <= r;
+        if (move) {
+          if (lane == 0) tab[r] = val;
+          r = nxt;
+          code = ncode;
+        }
+      }
+      __syncwarp();
+      if (be) break;
+      nbase = wrap(nbase + 32);
+    }
+    if (lane == 0) tab[r] = FH_EMPTY;
+    __syncwarp();
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Sorted queue in a power-of-two ring of uint64 keys: a[(head + i) & mask],
+// i in [0, n), ascending.  Used for the candidate queue (pops at the head)
+// and for the top-pq list (head fixed at 0).
+// ---------------------------------------------------------------------------
+struct SortedRing {
+  uint64_t *a;
+  int mask;
+
+  __device__ __forceinline__ uint64_t at(int head, int i) const { return a[(head + i) & mask]; }
+
+  // Number of keys < key (n <= 1024): 32 evenly spaced samples locate the
+  // stride, then one 32-wide window inside it.
+  __device__ __forceinline__ int lower_bound(int head, int n, uint64_t key, int lane) const {
+    if (n == 0) return 0;
+    int s = (n + 31) >> 5;
+    int i1 = lane * s;
+    bool lt1 = i1 < n && at(head, i1) < key;
+    int c = __popc(__ballot_sync(FULL, lt1));
+    if (c == 0) return 0;
+    int lo = (c - 1) * s + 1;
+    int hi = min(c * s, n);
+    int i2 = lo + lane;
+    bool lt2 = i2 < hi && at(head, i2) < key;
+    return lo + __popc(__ballot_sync(FULL, lt2));
+  }
+
+  // Insert at its sorted place; the keys after it move up one slot.
+  __device__ __forceinline__ void insert(int head, int &n, uint64_t key, int lane) {
+    int pos = lower_bound(head, n, key, lane);
+    for (int hi = n; hi > pos; hi -= 32) {
+      int lo = max(pos, hi - 32);
+      int i = lo + lane;
+      uint64_t v = 0;
+      if (i < hi) v = at(head, i);
+      __syncwarp();
+      if (i < hi) a[(head + i + 1) & mask] = v;
+      __syncwarp();
+    }
+    if (lane == 0) a[(head + pos) & mask] = key;
+    __syncwarp();
+    ++n;
+  }
+};
+
+}  // namespace song

@@ -1,0 +1,46 @@
+// internal.h -- declarations shared by the C-ABI layer and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace song {
+
+// Device layout of one resident index.
+struct DeviceIndex {
+  uint64_t n = 0;
+  int dim = 0;
+  int shift = 0;
+  int metric = 0;
+  int storage = 0;
+  int dpad = 0;             // elements per stored row (row_bytes / element size)
+  uint32_t row_bytes = 0;   // bytes per stored row, a multiple of 16
+  const void *rows = nullptr;        // n rows of row_bytes
+  const float *row_scale = nullptr;  // FP8: one scale per row
+  const float *rows_f32 = nullptr;   // FP32 rows (rerank; == rows for F32 storage)
+  uint32_t f32_row_bytes = 0;
+  const uint32_t *adj = nullptr;     // n << shift uint32: slot 0 = degree
+};
+
+struct SearchCall {
+  const float *queries = nullptr;  // nq x dim, device
+  int nq = 0;
+  int pq = 0;
+  int k = 0;
+  uint64_t *out = nullptr;         // nq x k, device
+  int32_t *hops = nullptr;         // nq or null
+  int32_t *evals = nullptr;        // nq or null
+  uint32_t *counter = nullptr;     // one uint32 of device scratch (work counter)
+  int32_t *error = nullptr;        // one int32 device error flag
+};
+
+// Launch the plain search.  Returns a cudaError_t-compatible code (0 ok) or
+// -1 when the shape is unsupported; sets *smem_per_warp if non-null.
+int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t stream);
+
+// Shared-memory bytes one warp needs for (ix, pq).
+uint32_t search_warp_bytes(const DeviceIndex &ix, int pq);
+
+int launch_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *out, cudaStream_t s);
+
+}  // namespace song
