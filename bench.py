@@ -36,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PQ_SWEEP = [50, 100, 150, 200, 250, 300, 350, 400, 500, 600, 800, 1000]
-CPU_K_SWEEP = [10, 15, 20, 30, 40, 60, 80, 100, 150, 200, 300]
+CPU_K_SWEEP = [10, 20, 40, 80, 150, 300, 500, 800, 1200, 1600, 2000]
 
 
 def log(*a):
@@ -375,7 +375,7 @@ def main():
     e2e = world * nq * args.steps / e2e_s
 
     # roofline: algorithmic bytes per launch / mean kernel time
-    row_bytes = 4 * ((w.dim + 3) // 4)
+    row_bytes = 4 * (((w.dim + 3) // 4) * 4)
     alg_bytes = int((4 * w.dim * nq) + hops.sum() * (1 << w.shift) * 4 + evals.sum() * row_bytes + nq * k * 8)
     mean_s = (sum(kernel_ms) / len(kernel_ms)) / 1000.0
     achieved = alg_bytes / mean_s / 1e9

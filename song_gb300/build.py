@@ -20,6 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(LIB_DIR, "libsong_gb300.so")
+CLI_PATH = os.path.join(LIB_DIR, "song")
 
 CUDA_SOURCES = ["search.cu", "capi.cu"]
 CXX_SOURCES = ["graph_build.cpp"]
@@ -90,6 +91,12 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         subprocess.check_call([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread",
                                "-L" + os.path.join(cuda_home(), "lib64")])
         os.replace(tmp, LIB_PATH)
+    cli_src = os.path.join(CSRC, "song_cli.cpp")
+    if force or _stale(CLI_PATH, [cli_src, LIB_PATH] + common_deps):
+        tmp = CLI_PATH + ".tmp%d" % os.getpid()
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, cli_src, "-o", tmp,
+                               "-L" + LIB_DIR, "-lsong_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"])
+        os.replace(tmp, CLI_PATH)
     return LIB_PATH
 
 

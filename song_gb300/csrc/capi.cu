@@ -105,7 +105,7 @@ int check_search_args(const song_index *ix, int nq, int pq, int k) {
   if (pq < 2 || pq > SONG_MAX_PQ) return fail(SONG_ERR_ARG, "pq must be in [2, %d]", SONG_MAX_PQ);
   if (k < 1 || k > pq) return fail(SONG_ERR_ARG, "k must be in [1, pq]");
   uint32_t wb = song::search_warp_bytes(ix->dx, pq);
-  if (wb * 4u > 227u * 1024u)
+  if (wb > 227u * 1024u)
     return fail(SONG_ERR_ARG, "pq %d with dim %d needs %u B of shared memory per warp", pq,
                 ix->dx.dim, wb);
   return SONG_OK;

@@ -34,13 +34,16 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "device_common.cuh"
 #include "internal.h"
+#include "reg_queue.cuh"
 
 namespace song {
 
-constexpr int WARPS_PER_BLOCK = 4;
+constexpr int MAX_WARPS_PER_BLOCK = 4;
 
 struct Params {
   const uint8_t *rows;
@@ -57,8 +60,8 @@ struct Params {
   uint32_t *counter;
   int32_t *error;
   uint32_t warp_bytes;
-  uint32_t off_mbar, off_cand, off_q, off_Q, off_T, off_hash;
-  int qmask, tmask, cap;
+  uint32_t off_mbar, off_cand, off_q, off_hash;
+  int cap;
   uint64_t magic;
 };
 
@@ -144,8 +147,17 @@ __device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage
   return true;
 }
 
-template <int METRIC, int H>
-__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t y = __shfl_xor_sync(FULL, x, o);
+    x = y < x ? y : x;
+  }
+  return x;
+}
+
+template <int METRIC, int H, int S>
+__global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1)
     search_kernel(const Params p) {
   extern __shared__ __align__(128) uint8_t smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -156,8 +168,7 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
   uint32_t *cbuf = reinterpret_cast<uint32_t *>(ws + p.off_cand);
   float *qv = reinterpret_cast<float *>(ws + p.off_q);
   VisitedHash vh{reinterpret_cast<int32_t *>(ws + p.off_hash), p.cap, p.magic};
-  SortedRing Q{reinterpret_cast<uint64_t *>(ws + p.off_Q), p.qmask};
-  SortedRing T{reinterpret_cast<uint64_t *>(ws + p.off_T), p.tmask};
+  RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
 
   if (lane == 0) {
     mbar_init(&mbar[0], 1);
@@ -177,6 +188,9 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
     const float *qsrc = p.queries + static_cast<size_t>(qid) * p.dim;
     for (int j = lane; j < p.dim; j += 32) qv[j] = qsrc[j];
     vh.clear(lane);
+    // Adjacency row of vertex 0, the first vertex popped.
+    uint32_t next_id = 0;
+    uint32_t a_next = lane < nslots ? __ldg(p.adj + lane) : 0u;
 
     // warp_astar_accelerator.h:115-176: distance to vertex 0, queue = {0}.
     float cd;
@@ -184,29 +198,31 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
       if (lane == 0) atomicOr(p.error, 1);
       return;
     }
-    const float d0 = __shfl_sync(FULL, cd, 0);
-    int qhead = 0, qn = 0, tn = 0;
-    Q.insert(qhead, qn, make_key(d0, 0u), lane);
+    int qn = 0, tn = 0;
+    Q.clear();
+    T.clear();
+    Q.insert(make_key(__shfl_sync(FULL, cd, 0), 0u), qn, lane);
     vh.add(0u, lane);
     int hops = 0, evals = 1;
 
     while (qn > 0) {
       // :186-193 pop the minimum, drop it from the visited hash.
-      const uint64_t now = Q.at(qhead, 0);
-      qhead = (qhead + 1) & p.qmask;
+      const uint64_t now = Q.get(0);
+      Q.pop_front(lane);
       --qn;
       const uint32_t now_id = key_id(now);
-      const uint32_t *arow = p.adj + (static_cast<uint64_t>(now_id) << p.shift);
-      const uint32_t a = lane < nslots ? __ldg(arow + lane) : 0u;
+      uint32_t a = a_next;
+      if (now_id != next_id)  // not taken: the prefetch predicts the pop exactly
+        a = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(now_id) << p.shift) + lane) : 0u;
       vh.del(now_id, lane);
       // :191 finish test (<=) against the list maximum.
-      if (tn == p.pq && key_dist(T.at(0, tn - 1)) <= key_dist(now)) break;
+      if (tn == p.pq && key_dist(T.get(tn - 1)) <= key_dist(now)) break;
       ++hops;
       // :198-210 move it to the top-pq list.
-      T.insert(0, tn, now, lane);
+      T.insert(now, tn, lane);
       vh.add(now_id, lane);
       if (tn > p.pq) {
-        const uint64_t ev = T.at(0, tn - 1);
+        const uint64_t ev = T.get(tn - 1);
         vh.del(key_id(ev), lane);
         --tn;
       }
@@ -225,16 +241,28 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
         return;
       }
       evals += m;
+      // The next vertex popped is the smaller of the queue head and the best
+      // candidate (the select-insert rule can only reject candidates above a
+      // full queue's maximum); start loading its adjacency row now so that it
+      // arrives while the candidates are inserted.
+      const uint64_t ck = lane < m ? make_key(cd, cid) : ~0ull;
+      const uint64_t cmin = warp_min_u64(ck);
+      const uint64_t qh = qn > 0 ? Q.get(0) : ~0ull;
+      const uint64_t nk = cmin < qh ? cmin : qh;
+      if (nk != ~0ull) {
+        next_id = key_id(nk);
+        a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
+      }
       // :297-322 select-insert in candidate order.
       for (int c = 0; c < m; ++c) {
         const float d = __shfl_sync(FULL, cd, c);
         const uint32_t id = __shfl_sync(FULL, cid, c);
         const uint64_t key = make_key(d, id);
-        if (qn >= p.pq && key_dist(Q.at(qhead, qn - 1)) < key_dist(key)) continue;
-        Q.insert(qhead, qn, key, lane);
+        if (qn >= p.pq && key_dist(Q.get(qn - 1)) < key_dist(key)) continue;
+        Q.insert(key, qn, lane);
         vh.add(id, lane);
         if (qn >= p.pq + 1) {
-          const uint64_t ev = Q.at(qhead, qn - 1);
+          const uint64_t ev = Q.get(qn - 1);
           vh.del(key_id(ev), lane);
           --qn;
         }
@@ -242,8 +270,11 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
     }
     // :331-335 ascending ids; slots past the list length get UINT64_MAX.
     uint64_t *o = p.out + static_cast<size_t>(qid) * p.k;
-    for (int i = lane; i < p.k; i += 32)
-      o[i] = i < tn ? static_cast<uint64_t>(key_id(T.at(0, i))) : ~0ull;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      const int i = lane * S + j;
+      if (i < p.k) o[i] = i < tn ? static_cast<uint64_t>(key_id(T.v[j])) : ~0ull;
+    }
     if (lane == 0) {
       if (p.hops) p.hops[qid] = hops;
       if (p.evals) p.evals[qid] = evals;
@@ -266,29 +297,25 @@ namespace {
 
 uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
-int pow2_at_least(int x) {
-  int p = 1;
-  while (p < x) p <<= 1;
-  return p;
-}
+// Rows staged per buffer half: a typical hop evaluates 2-5 neighbours.
+int stage_rows(uint32_t row_bytes) { return row_bytes <= 1024 ? 4 : 2; }
 
-// Rows staged per buffer: enough rows for a typical hop, a few KB per warp.
-int stage_rows(uint32_t row_bytes) {
-  if (row_bytes <= 256) return 8;
-  if (row_bytes <= 1024) return 4;
-  return 2;
+// Register-queue segment: smallest power of two S with 32*S >= pq + 1.
+int queue_segment(int pq) {
+  int s = 1;
+  while (32 * s < pq + 1) s <<= 1;
+  return s;
 }
 
 struct Layout {
-  uint32_t warp_bytes, off_mbar, off_cand, off_q, off_Q, off_T, off_hash;
-  int qcap, tcap, cap, H;
+  uint32_t warp_bytes, off_mbar, off_cand, off_q, off_hash;
+  int cap, H, S;
 };
 
 Layout make_layout(const DeviceIndex &ix, int pq) {
   Layout L;
   L.H = stage_rows(ix.row_bytes);
-  L.qcap = pow2_at_least(pq + 1);
-  L.tcap = pow2_at_least(pq + 1);
+  L.S = queue_segment(pq);
   L.cap = 8 * pq;
   uint32_t off = 2u * L.H * ix.row_bytes;
   off = align_up(off, 16);
@@ -299,17 +326,59 @@ Layout make_layout(const DeviceIndex &ix, int pq) {
   off = align_up(off, 16);
   L.off_q = off;
   off += align_up(static_cast<uint32_t>(ix.dim) * 4u, 16);
-  L.off_Q = off;
-  off += 8u * L.qcap;
-  L.off_T = off;
-  off += 8u * L.tcap;
   L.off_hash = off;
   off += 4u * L.cap;
   L.warp_bytes = align_up(off, 128);
   return L;
 }
 
-template <int METRIC, int H>
+// Launch shape per (kernel, bytes per warp): the warps-per-block in {4, 2, 1}
+// that keeps the most warps resident per SM.
+struct Shape {
+  const void *fn;
+  uint32_t warp_bytes;
+  int wpb, blocks_per_sm, sms;
+};
+
+std::mutex g_shape_mu;
+std::vector<Shape> g_shapes;
+
+int get_shape(const void *fn, uint32_t warp_bytes, Shape &out) {
+  std::lock_guard<std::mutex> lk(g_shape_mu);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  for (const Shape &s : g_shapes)
+    if (s.fn == fn && s.warp_bytes == warp_bytes) {
+      out = s;
+      return 0;
+    }
+  int sms = 0, optin = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // One kernel serves indexes and pq values of different footprints, so its
+  // dynamic shared-memory limit is raised once to the device maximum rather
+  // than to the size of any one launch.
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e != cudaSuccess) return e;
+  Shape best{fn, warp_bytes, 0, 0, sms};
+  for (int wpb = MAX_WARPS_PER_BLOCK; wpb >= 1; wpb >>= 1) {
+    const size_t smem = static_cast<size_t>(warp_bytes) * wpb;
+    if (smem > static_cast<size_t>(optin)) continue;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, wpb * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm * wpb > best.blocks_per_sm * best.wpb) {
+      best.wpb = wpb;
+      best.blocks_per_sm = per_sm;
+    }
+  }
+  if (best.wpb == 0) return -1;
+  g_shapes.push_back(best);
+  out = best;
+  return 0;
+}
+
+template <int METRIC, int H, int S>
 int launch_t(const DeviceIndex &ix, const SearchCall &c, const Layout &L, cudaStream_t stream) {
   Params p;
   p.rows = static_cast<const uint8_t *>(ix.rows);
@@ -331,40 +400,38 @@ int launch_t(const DeviceIndex &ix, const SearchCall &c, const Layout &L, cudaSt
   p.off_mbar = L.off_mbar;
   p.off_cand = L.off_cand;
   p.off_q = L.off_q;
-  p.off_Q = L.off_Q;
-  p.off_T = L.off_T;
   p.off_hash = L.off_hash;
-  p.qmask = L.qcap - 1;
-  p.tmask = L.tcap - 1;
   p.cap = L.cap;
   p.magic = ~0ull / static_cast<uint64_t>(L.cap);
 
-  const size_t smem = static_cast<size_t>(L.warp_bytes) * WARPS_PER_BLOCK;
-  auto kern = search_kernel<METRIC, H>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS_PER_BLOCK * 32, smem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) return -1;
-  const int want = (c.nq + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
-  const int grid = std::max(1, std::min(want, per_sm * sms));
-  e = cudaMemsetAsync(c.counter, 0, sizeof(uint32_t), stream);
-  if (e != cudaSuccess) return e;
-  kern<<<grid, WARPS_PER_BLOCK * 32, smem, stream>>>(p);
+  auto kern = search_kernel<METRIC, H, S>;
+  Shape sh;
+  int e = get_shape(reinterpret_cast<const void *>(kern), L.warp_bytes, sh);
+  if (e != 0) return e;
+  const int want = (c.nq + sh.wpb - 1) / sh.wpb;
+  const int grid = std::max(1, std::min(want, sh.blocks_per_sm * sh.sms));
+  cudaError_t ce = cudaMemsetAsync(c.counter, 0, sizeof(uint32_t), stream);
+  if (ce != cudaSuccess) return ce;
+  kern<<<grid, sh.wpb * 32, static_cast<size_t>(L.warp_bytes) * sh.wpb, stream>>>(p);
   return cudaGetLastError();
+}
+
+template <int METRIC, int H>
+int launch_s(const DeviceIndex &ix, const SearchCall &c, const Layout &L, cudaStream_t s) {
+  switch (L.S) {
+    case 1: return launch_t<METRIC, H, 1>(ix, c, L, s);
+    case 2: return launch_t<METRIC, H, 2>(ix, c, L, s);
+    case 4: return launch_t<METRIC, H, 4>(ix, c, L, s);
+    case 8: return launch_t<METRIC, H, 8>(ix, c, L, s);
+    case 16: return launch_t<METRIC, H, 16>(ix, c, L, s);
+    case 32: return launch_t<METRIC, H, 32>(ix, c, L, s);
+    default: return -1;
+  }
 }
 
 template <int METRIC>
 int launch_m(const DeviceIndex &ix, const SearchCall &c, const Layout &L, cudaStream_t s) {
-  switch (L.H) {
-    case 8: return launch_t<METRIC, 8>(ix, c, L, s);
-    case 4: return launch_t<METRIC, 4>(ix, c, L, s);
-    default: return launch_t<METRIC, 2>(ix, c, L, s);
-  }
+  return L.H == 4 ? launch_s<METRIC, 4>(ix, c, L, s) : launch_s<METRIC, 2>(ix, c, L, s);
 }
 
 }  // namespace

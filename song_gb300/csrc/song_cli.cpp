@@ -1,0 +1,178 @@
+// song_cli.cpp -- command-line driver with the reference's argv and output
+// (main.cu:49-100), on top of the C ABI in include/song_gb300.h.
+//
+//   song build <build_data> <query_data> <search_top_k> <row> <dim> <return_top_k> <l2|ip|cos>
+//   song test  <build_data> <query_data> <search_top_k> <row> <dim> <return_top_k> <l2|ip|cos>
+//
+// build: reads one-based LIBSVM vectors (parser.h:12-66), builds the graph
+//        (graph.h:149-167) and writes bfsg.graph / bfsg.data in the working
+//        directory (main.cu:78-85).
+// test:  loads bfsg.graph / bfsg.data, reads the queries, searches them in one
+//        batch (main.cu:23-35, 86-94) and prints the first return_top_k
+//        zero-based ids of each query on one line, "%zu " per id.
+//
+// The reference bakes pq_size into the binary (fill_parameters.sh:12,35-53)
+// and ignores search_top_k in GPU mode; here pq_size is search_top_k, or
+// SONG_PQ_SIZE when set.  Graph constants follow KernelFixedDegreeGraph
+// (kernelgraph.h:27-29: shift 5, degree 15, row capacity 31) unless
+// SONG_SHIFT / SONG_SEARCH_DEGREE / SONG_FIXED_DEGREE are set.
+// SONG_BUILD_DIV > 0 selects the batch-parallel build.
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <utility>
+#include <vector>
+
+#include "song_gb300.h"
+
+namespace {
+
+int env_int(const char *name, int dflt) {
+  const char *v = getenv(name);
+  return v && *v ? atoi(v) : dflt;
+}
+
+// parser.h:24-64: separators are ':' and ' '; pairs (index after a space,
+// value after a colon); one-based indices; values read as double, stored as
+// float.  Returns false on an unreadable file.
+bool parse_libsvm(const char *path, int dim, std::vector<std::vector<std::pair<int, float>>> &rows,
+                  std::string &err) {
+  FILE *fp = fopen(path, "r");
+  if (!fp) {
+    err = std::string("File not found at (") + path + ")";
+    return false;
+  }
+  const int MAX_LINE = 10000000;
+  std::vector<char> buf(MAX_LINE);
+  while (fgets(buf.data(), MAX_LINE, fp)) {
+    std::vector<int> tok;
+    for (int i = 0; buf[i] != '\0'; ++i)
+      if (buf[i] == ':' || buf[i] == ' ') tok.push_back(i);
+    std::vector<std::pair<int, float>> r;
+    for (size_t i = 0; i + 1 < tok.size(); i += 2) {
+      int index = 0;
+      double v = 0;
+      sscanf(buf.data() + tok[i] + 1, "%d", &index);
+      sscanf(buf.data() + tok[i + 1] + 1, "%lf", &v);
+      index -= 1;
+      if (index < 0 || index >= dim) {
+        fclose(fp);
+        err = "feature index out of range in " + std::string(path);
+        return false;
+      }
+      r.push_back(std::make_pair(index, static_cast<float>(v)));
+    }
+    rows.push_back(std::move(r));
+  }
+  fclose(fp);
+  return true;
+}
+
+void densify(const std::vector<std::vector<std::pair<int, float>>> &rows, int dim, size_t n,
+             std::vector<float> &out) {
+  out.assign(n * static_cast<size_t>(dim), 0.0f);
+  for (size_t i = 0; i < rows.size() && i < n; ++i)
+    for (const auto &p : rows[i]) out[i * dim + p.first] = p.second;
+}
+
+void usage(char **argv) {
+  printf("Usage: %s <build/test> <build_data> <query_data> <search_top_k> <row> <dim> <return_top_k> <l2/ip/cos>\n",
+         argv[0]);
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc != 9) {
+    usage(argv);
+    return 1;
+  }
+  const uint64_t row = strtoull(argv[5], nullptr, 10);
+  const int dim = atoi(argv[6]);
+  const int display = atoi(argv[7]);
+  const std::string dt = argv[8];
+  int metric;
+  if (dt == "l2") metric = SONG_METRIC_L2;
+  else if (dt == "ip") metric = SONG_METRIC_IP;
+  else if (dt == "cos") metric = SONG_METRIC_COS;
+  else {
+    usage(argv);
+    return 1;
+  }
+  const std::string mode = argv[1];
+  const int shift = env_int("SONG_SHIFT", 5);
+  const int search_degree = env_int("SONG_SEARCH_DEGREE", 15);
+  const int fixed_degree = env_int("SONG_FIXED_DEGREE", (1 << shift) - 1);
+  std::string err;
+  if (mode == "build") {
+    std::vector<std::vector<std::pair<int, float>>> rows;
+    if (!parse_libsvm(argv[2], dim, rows, err)) {
+      fprintf(stderr, "%s\n", err.c_str());
+      return 1;
+    }
+    std::vector<float> data;
+    densify(rows, dim, row, data);
+    std::vector<uint64_t> graph(static_cast<size_t>(row) << shift);
+    fprintf(stderr, "Writing the graph and data...");
+    int rc = song_graph_build(data.data(), row, dim, metric, shift, search_degree, fixed_degree, 150,
+                              env_int("SONG_BUILD_DIV", 0),
+                              static_cast<int>(std::thread::hardware_concurrency()), graph.data());
+    if (rc) {
+      fprintf(stderr, "\n%s: %s\n", song_status_string(rc), song_last_error());
+      return 1;
+    }
+    FILE *fd = fopen("bfsg.data", "wb");
+    FILE *fg = fopen("bfsg.graph", "wb");
+    if (!fd || !fg) {
+      fprintf(stderr, "\ncannot write bfsg.data / bfsg.graph\n");
+      return 1;
+    }
+    fwrite(data.data(), sizeof(float), data.size(), fd);
+    fwrite(graph.data(), sizeof(uint64_t), graph.size(), fg);
+    fclose(fd);
+    fclose(fg);
+    fprintf(stderr, "done\n");
+    return 0;
+  }
+  if (mode == "test") {
+    fprintf(stderr, "Loading the graph and data...");
+    song_index *ix = nullptr;
+    int rc = song_index_load("bfsg.graph", "bfsg.data", row, dim, shift, metric, SONG_STORAGE_F32, 0, &ix);
+    if (rc) {
+      fprintf(stderr, "\n%s: %s\n", song_status_string(rc), song_last_error());
+      return 1;
+    }
+    fprintf(stderr, "done\n");
+    std::vector<std::vector<std::pair<int, float>>> rows;
+    if (!parse_libsvm(argv[3], dim, rows, err)) {
+      fprintf(stderr, "%s\n", err.c_str());
+      song_index_free(ix);
+      return 1;
+    }
+    std::vector<float> q;
+    densify(rows, dim, rows.size(), q);
+    const int pq = env_int("SONG_PQ_SIZE", atoi(argv[4]));
+    const int nq = static_cast<int>(rows.size());
+    std::vector<uint64_t> out(static_cast<size_t>(nq) * pq);
+    rc = song_search(ix, q.data(), nq, pq, pq, out.data(), nullptr, nullptr);
+    song_index_free(ix);
+    if (rc) {
+      fprintf(stderr, "%s: %s\n", song_status_string(rc), song_last_error());
+      return 1;
+    }
+    for (int i = 0; i < nq; ++i) {
+      for (int j = 0; j < pq && j < display; ++j) {
+        uint64_t id = out[static_cast<size_t>(i) * pq + j];
+        if (id == UINT64_MAX) break;
+        printf("%zu ", static_cast<size_t>(id));
+      }
+      printf("\n");
+    }
+    return 0;
+  }
+  usage(argv);
+  return 1;
+}
