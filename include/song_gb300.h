@@ -121,6 +121,23 @@ int song_graph_build(const float *data, uint64_t n, int dim, int metric, int shi
                      int search_degree, int fixed_degree, int budget, int batch_div, int nthreads,
                      uint64_t *graph_out);
 
+/* Size of the fixed device scratch array used by song_search_noalloc. */
+#define SONG_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* song_search without any device allocation.  No counterpart in the
+ * reference: for callers that cannot let a library call cudaMalloc (a service
+ * whose GPU memory is already owned by its own pool or budget, or a request
+ * path that must not pay for an allocation that may synchronise the device).
+ * Host buffers as in song_search; the device copies of queries and ids and
+ * the kernel's work counter and error flag live in one file-scope device
+ * array of SONG_NOALLOC_SCRATCH_BYTES per GPU, held until process exit.  A
+ * batch may use 256 + round_up(nq*dim*4, 256) + nq*k*8 bytes of it; larger
+ * batches return SONG_ERR_ARG.  The array's device address is looked up on
+ * the first call on each device (make that call before any stream capture).
+ * Calls overlapping on one GPU share the array and race: serialise them. */
+int song_search_noalloc(song_index *index, const float *queries, int nq, int pq, int k,
+                        uint64_t *out);
+
 /* The visited-hash slot function of the reference's default build
  * (fixhash.h:20-24) evaluated on the device for `count` ids, for tests. */
 int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_out);

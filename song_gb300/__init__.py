@@ -31,7 +31,7 @@ NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 EXPORTED = [
     "song_status_string", "song_last_error", "song_index_create", "song_index_load",
     "song_index_free", "song_index_info", "song_search", "song_search_device",
-    "song_astar_search_batch", "song_graph_build", "song_debug_fixhash",
+    "song_astar_search_batch", "song_graph_build", "song_debug_fixhash", "song_search_noalloc",
 ]
 
 
@@ -80,6 +80,8 @@ def load_library():
     L.song_astar_search_batch.argtypes = [P, i32, i32, P, P, P, i32, u64, i32, i32]
     L.song_graph_build.restype = i32
     L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
+    L.song_search_noalloc.restype = i32
+    L.song_search_noalloc.argtypes = [P, P, i32, i32, i32, P]
     L.song_debug_fixhash.restype = i32
     L.song_debug_fixhash.argtypes = [P, i32, i32, P]
     _lib = L
@@ -154,6 +156,15 @@ class Index:
         evals = np.empty(nq, dtype=np.int32) if stats else None
         _check(load_library().song_search(self._h, _ptr(q), nq, pq, k, _ptr(out), _ptr(hops), _ptr(evals)))
         return (out, hops, evals) if stats else out
+
+    def search_noalloc(self, queries, pq, k=None):
+        """song_search_noalloc: the host-buffer search that allocates no device
+        memory (scratch in a fixed 16 MiB device array per GPU)."""
+        k = pq if k is None else k
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        out = np.empty((q.shape[0], k), dtype=np.uint64)
+        _check(load_library().song_search_noalloc(self._h, _ptr(q), q.shape[0], pq, k, _ptr(out)))
+        return out
 
     def search_device(self, q_ptr, nq, pq, k, out_ptr, hops_ptr=None, evals_ptr=None, stream=None):
         """Device-buffer search (song_search_device): raw device pointers

@@ -22,7 +22,7 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(LIB_DIR, "libsong_gb300.so")
 CLI_PATH = os.path.join(LIB_DIR, "song")
 
-CUDA_SOURCES = ["search.cu", "capi.cu"]
+CUDA_SOURCES = ["search.cu", "capi.cu", "noalloc.cu"]
 CXX_SOURCES = ["graph_build.cpp"]
 HEADERS = ["device_common.cuh", "internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

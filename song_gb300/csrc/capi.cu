@@ -12,29 +12,11 @@
 #include "internal.h"
 #include "song_gb300.h"
 
-struct song_index {
-  int device = 0;
-  song::DeviceIndex dx;
-  void *d_rows = nullptr;
-  uint32_t *d_adj = nullptr;
-  float *d_scale = nullptr;
-  float *d_rows_f32 = nullptr;
-  uint32_t *d_counter = nullptr;
-  int32_t *d_error = nullptr;
-  cudaStream_t stream = nullptr;
-  // device staging for the host-buffer entry point
-  float *d_q = nullptr;
-  size_t cap_q = 0;
-  uint64_t *d_out = nullptr;
-  size_t cap_out = 0;
-  int32_t *d_stats = nullptr;
-  size_t cap_stats = 0;
-  uint64_t device_bytes = 0;
-};
-
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace song {
 
 int fail(int code, const char *fmt, ...) {
   char buf[512];
@@ -45,6 +27,26 @@ int fail(int code, const char *fmt, ...) {
   g_last_error = buf;
   return code;
 }
+
+void clear_error() { g_last_error.clear(); }
+
+int check_search_args(const song_index *ix, int nq, int pq, int k) {
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (nq < 0) return fail(SONG_ERR_ARG, "nq must be >= 0");
+  if (pq < 2 || pq > SONG_MAX_PQ) return fail(SONG_ERR_ARG, "pq must be in [2, %d]", SONG_MAX_PQ);
+  if (k < 1 || k > pq) return fail(SONG_ERR_ARG, "k must be in [1, pq]");
+  uint32_t wb = search_warp_bytes(ix->dx, pq);
+  if (wb > 227u * 1024u)
+    return fail(SONG_ERR_ARG, "pq %d with dim %d needs %u B of shared memory per warp", pq,
+                ix->dx.dim, wb);
+  return SONG_OK;
+}
+
+}  // namespace song
+
+namespace {
+using song::fail;
+using song::check_search_args;
 
 #define SONG_CUDA(call)                                                                   \
   do {                                                                                    \
@@ -97,18 +99,6 @@ void release(song_index *ix) {
   cudaFree(ix->d_stats);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;
-}
-
-int check_search_args(const song_index *ix, int nq, int pq, int k) {
-  if (!ix) return fail(SONG_ERR_ARG, "null index");
-  if (nq < 0) return fail(SONG_ERR_ARG, "nq must be >= 0");
-  if (pq < 2 || pq > SONG_MAX_PQ) return fail(SONG_ERR_ARG, "pq must be in [2, %d]", SONG_MAX_PQ);
-  if (k < 1 || k > pq) return fail(SONG_ERR_ARG, "k must be in [1, pq]");
-  uint32_t wb = song::search_warp_bytes(ix->dx, pq);
-  if (wb > 227u * 1024u)
-    return fail(SONG_ERR_ARG, "pq %d with dim %d needs %u B of shared memory per warp", pq,
-                ix->dx.dim, wb);
-  return SONG_OK;
 }
 
 int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_out,

@@ -44,3 +44,34 @@ uint32_t search_warp_bytes(const DeviceIndex &ix, int pq);
 int launch_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *out, cudaStream_t s);
 
 }  // namespace song
+
+struct song_index;
+
+namespace song {
+// Error reporting of the C ABI (capi.cu): records the message for
+// song_last_error() on the calling thread and returns `code`.
+int fail(int code, const char *fmt, ...);
+void clear_error();
+int check_search_args(const song_index *ix, int nq, int pq, int k);
+}  // namespace song
+
+// The opaque handle of include/song_gb300.h.
+struct song_index {
+  int device = 0;
+  song::DeviceIndex dx;
+  void *d_rows = nullptr;
+  uint32_t *d_adj = nullptr;
+  float *d_scale = nullptr;
+  float *d_rows_f32 = nullptr;
+  uint32_t *d_counter = nullptr;
+  int32_t *d_error = nullptr;
+  cudaStream_t stream = nullptr;
+  // device staging for the host-buffer entry point song_search
+  float *d_q = nullptr;
+  size_t cap_q = 0;
+  uint64_t *d_out = nullptr;
+  size_t cap_out = 0;
+  int32_t *d_stats = nullptr;
+  size_t cap_stats = 0;
+  uint64_t device_bytes = 0;
+};
