@@ -58,6 +58,7 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cache", default=os.environ.get("SONG_CACHE", "/tmp/song_gb300_cache"))
+    p.add_argument("--curve", action="store_true", help="time every pq of the sweep (recall/throughput curve)")
     return p.parse_args()
 
 
@@ -293,17 +294,26 @@ def main():
     # pq sweep: smallest pq whose tie-aware recall@10 reaches the target
     sweep = []
     pq = args.pq
-    if pq == 0:
+    if pq == 0 or args.curve:
         for cand in PQ_SWEEP:
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
             search(cand)
+            t0.record(stream)
+            reps = 3 if args.curve else 1
+            for _ in range(reps):
+                search(cand)
+            t1.record(stream)
             torch.cuda.synchronize()
+            qps = reps * nq / (t0.elapsed_time(t1) / 1000.0)
             ids = dout.cpu().numpy().view(np.uint64)
             r = GT.recall_tie_aware(ids, data, queries, gt_kth, w.metric, k)
-            sweep.append([cand, round(r, 4)])
-            log("[bench] pq %d recall@10 %.4f" % (cand, r))
-            if r >= args.recall:
+            sweep.append([cand, round(r, 4), round(qps, 1)])
+            log("[bench] pq %d recall@10 %.4f  %.0f q/s" % (cand, r, qps))
+            if pq == 0 and r >= args.recall:
                 pq = cand
-                break
+                if not args.curve:
+                    break
         if pq == 0:
             pq = PQ_SWEEP[-1]
     search(pq, stats=True)
@@ -421,7 +431,7 @@ def main():
                        "graph": "shift %d (FIXED_DEGREE %d, SEARCH_DEGREE %d), batch-parallel build div %d"
                                 % (w.shift, w.fixed_degree, w.search_degree, args.build_div),
                        "pq": pq, "top_k": k, "queries_per_step": nq, "recall_at_10": round(rec, 4),
-                       "recall_at_10_ids": round(rec_ids, 4), "pq_sweep": sweep,
+                       "recall_at_10_ids": round(rec_ids, 4), "pq_sweep_recall_qps": sweep,
                        "mean_hops": round(float(hops.mean()), 2), "mean_evals": round(float(evals.mean()), 2),
                        "l2": "flushed between steps (256 MB write); index 512 MB > L2",
                        "parallelism": "replicas" if world > 1 else "single GPU"},

@@ -121,6 +121,64 @@ int song_graph_build(const float *data, uint64_t n, int dim, int metric, int shi
                      int search_degree, int fixed_degree, int budget, int batch_div, int nthreads,
                      uint64_t *graph_out);
 
+/* Low-precision storage (BF16 / FP8): number of the best final candidates
+ * re-ranked with exact FP32 distances before the first k are returned.
+ * -1 (default) = all pq, 0 = none (results in the storage's precision).
+ * No counterpart in the reference. */
+int song_index_set_rerank(song_index *index, int rerank);
+
+/* Stored rows (bytes as searched: F32, BF16, or FP8 bytes followed by the
+ * row's float scale), rows first .. first+count-1; *row_bytes gets the row
+ * size (out may be NULL to query it).  No counterpart in the reference. */
+int song_index_rows(const song_index *index, uint64_t first, uint64_t count, void *out,
+                    size_t out_bytes, int *row_bytes);
+
+/* Learned early exit (no counterpart in the reference).  A network
+ * 5 -> 32 -> 32 -> 1 (ReLU) reads, after every `every`-th hop from hop
+ * `min_hops` on, the query's state (log hop count, k-th and best list
+ * distance and queue-head gap relative to the start distance, log distance
+ * evaluations) and stops the search when its logit >= threshold; queries it
+ * never trusts run the plain search to its finish rule.  weights: the
+ * SONG_MLP_PARAMS FP32 parameters (W1[32][5], b1[32], W2[32][32], b2[32],
+ * w3[32], b3), stored on the device in BF16; NULL switches the exit off.
+ * F32 and BF16 storage. */
+#define SONG_MLP_PARAMS 1281
+int song_index_set_early_exit(song_index *index, const float *weights, float threshold,
+                              int min_hops, int every);
+
+/* Fixed hop budget (0 = off): stop every query after max_hops expansions.
+ * A baseline heuristic to compare the learned exit against; no counterpart
+ * in the reference.  F32 and BF16 storage. */
+int song_index_set_hop_limit(song_index *index, int max_hops);
+
+/* Training of the early-exit network (no counterpart in the reference), all
+ * buffers on the device, ordered on `stream`: x n x 5 features, y n labels
+ * (0/1), w n sample weights or NULL, perm epochs x n sample indices or NULL
+ * (in order), Adam with learning rate lr on minibatches of `batch`, loss
+ * weighted binary cross-entropy on the logit.  params (SONG_MLP_PARAMS FP32)
+ * are read as the start point and overwritten; loss (epochs floats, may be
+ * NULL) receives the mean minibatch loss of each epoch. */
+int song_mlp_train_device(const float *d_x, const float *d_y, const float *d_w, int64_t n,
+                          const int32_t *d_perm, int epochs, int batch, float lr, float *d_params,
+                          float *d_loss, void *stream);
+
+/* Mean gradient and loss of the training objective over n samples (host
+ * buffers; w may be NULL), computed by the training kernels.  For checks. */
+int song_mlp_grad(const float *x, const float *y, const float *w, int n, const float *params,
+                  float *grad_out, float *loss_out);
+
+/* Logits of n samples (host buffers), FP32 weights, by the training kernels. */
+int song_mlp_forward(const float *x, int n, const float *params, float *logits_out);
+
+/* The plain search with per-hop tracing, DEVICE buffers on `stream`: for
+ * query q and hop h < trace_hops, trace[(q*trace_hops + h)*6 + 0..4] are the
+ * early-exit features after hop h+1 and [.. + 5] the number of changes of the
+ * top-k set so far; final[2q] = that count at the end, final[2q+1] = hops
+ * traced.  A hop's label "top-k already final" is trace[..5] == final[2q]. */
+int song_search_trace_device(song_index *index, const float *d_queries, int nq, int pq, int k,
+                             int trace_hops, float *d_trace, int32_t *d_final, uint64_t *d_out,
+                             int32_t *d_hops, int32_t *d_evals, void *stream);
+
 /* Size of the fixed device scratch array used by song_search_noalloc. */
 #define SONG_NOALLOC_SCRATCH_BYTES (16u << 20)
 

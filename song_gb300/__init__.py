@@ -32,7 +32,11 @@ EXPORTED = [
     "song_status_string", "song_last_error", "song_index_create", "song_index_load",
     "song_index_free", "song_index_info", "song_search", "song_search_device",
     "song_astar_search_batch", "song_graph_build", "song_debug_fixhash", "song_search_noalloc",
+    "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
+    "song_index_set_hop_limit", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
 ]
+MLP_PARAMS = 1281
+TRACE_FIELDS = 6
 
 
 class SongError(RuntimeError):
@@ -80,6 +84,22 @@ def load_library():
     L.song_astar_search_batch.argtypes = [P, i32, i32, P, P, P, i32, u64, i32, i32]
     L.song_graph_build.restype = i32
     L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
+    L.song_index_set_rerank.restype = i32
+    L.song_index_set_rerank.argtypes = [P, i32]
+    L.song_index_rows.restype = i32
+    L.song_index_rows.argtypes = [P, u64, u64, P, ctypes.c_size_t, ctypes.POINTER(i32)]
+    L.song_index_set_early_exit.restype = i32
+    L.song_index_set_early_exit.argtypes = [P, P, ctypes.c_float, i32, i32]
+    L.song_search_trace_device.restype = i32
+    L.song_search_trace_device.argtypes = [P, P, i32, i32, i32, i32, P, P, P, P, P, P]
+    L.song_index_set_hop_limit.restype = i32
+    L.song_index_set_hop_limit.argtypes = [P, i32]
+    L.song_mlp_train_device.restype = i32
+    L.song_mlp_train_device.argtypes = [P, P, P, ctypes.c_int64, P, i32, i32, ctypes.c_float, P, P, P]
+    L.song_mlp_grad.restype = i32
+    L.song_mlp_grad.argtypes = [P, P, P, i32, P, P, P]
+    L.song_mlp_forward.restype = i32
+    L.song_mlp_forward.argtypes = [P, i32, P, P]
     L.song_search_noalloc.restype = i32
     L.song_search_noalloc.argtypes = [P, P, i32, i32, i32, P]
     L.song_debug_fixhash.restype = i32
@@ -156,6 +176,42 @@ class Index:
         evals = np.empty(nq, dtype=np.int32) if stats else None
         _check(load_library().song_search(self._h, _ptr(q), nq, pq, k, _ptr(out), _ptr(hops), _ptr(evals)))
         return (out, hops, evals) if stats else out
+
+    def set_rerank(self, rerank):
+        """BF16/FP8 storage: FP32 re-rank of the best `rerank` final candidates
+        (-1 = all pq, 0 = none)."""
+        _check(load_library().song_index_set_rerank(self._h, int(rerank)))
+
+    def rows(self, first=0, count=None):
+        """Stored rows as raw bytes (count x row_bytes uint8)."""
+        L = load_library()
+        rb = ctypes.c_int()
+        _check(L.song_index_rows(self._h, 0, 0, None, 0, ctypes.byref(rb)))
+        count = self.n - first if count is None else count
+        out = np.empty((count, rb.value), dtype=np.uint8)
+        _check(L.song_index_rows(self._h, first, count, _ptr(out), out.nbytes, ctypes.byref(rb)))
+        return out
+
+    def set_early_exit(self, weights, threshold=0.0, min_hops=8, every=1):
+        """Attach the early-exit network (MLP_PARAMS FP32 weights) or detach it (None)."""
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+        if w is not None and w.size != MLP_PARAMS:
+            raise ValueError("expected %d weights" % MLP_PARAMS)
+        _check(load_library().song_index_set_early_exit(self._h, _ptr(w), float(threshold), int(min_hops), int(every)))
+
+    def set_hop_limit(self, max_hops):
+        """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""
+        _check(load_library().song_index_set_hop_limit(self._h, int(max_hops)))
+
+    def trace_device(self, q_ptr, nq, pq, k, trace_hops, trace_ptr, final_ptr, out_ptr,
+                     hops_ptr=None, evals_ptr=None, stream=None):
+        """Plain search with per-hop feature tracing (device pointers)."""
+        _check(load_library().song_search_trace_device(
+            self._h, ctypes.c_void_p(q_ptr), nq, pq, k, trace_hops, ctypes.c_void_p(trace_ptr),
+            ctypes.c_void_p(final_ptr), ctypes.c_void_p(out_ptr),
+            ctypes.c_void_p(hops_ptr) if hops_ptr else None,
+            ctypes.c_void_p(evals_ptr) if evals_ptr else None,
+            ctypes.c_void_p(stream) if stream else None))
 
     def search_noalloc(self, queries, pq, k=None):
         """song_search_noalloc: the host-buffer search that allocates no device
@@ -235,3 +291,79 @@ def read_bfsg(graph_path, data_path, n, dim, shift):
     graph = np.fromfile(graph_path, dtype=np.uint64, count=n << shift)
     data = np.fromfile(data_path, dtype=np.float32, count=n * dim).reshape(n, dim)
     return graph, data
+
+
+# ---------------------------------------------------------------------------
+# Decoding of stored low-precision rows (for inspection and tests)
+# ---------------------------------------------------------------------------
+
+def _e4m3_table():
+    t = np.zeros(256, dtype=np.float32)
+    for b in range(256):
+        sgn = -1.0 if b & 0x80 else 1.0
+        e = (b >> 3) & 0xF
+        m = b & 0x7
+        if e == 0xF and m == 0x7:
+            t[b] = np.nan
+        elif e == 0:
+            t[b] = sgn * (m / 8.0) * 2.0 ** -6
+        else:
+            t[b] = sgn * (1.0 + m / 8.0) * 2.0 ** (e - 7)
+    return t
+
+
+E4M3 = _e4m3_table()
+
+
+def dequantize_rows(raw, storage, dim):
+    """FP32 values the kernel computes with, from Index.rows() bytes."""
+    st = _storage(storage)
+    if st == 0:
+        return raw.view(np.float32)[:, :dim].copy()
+    if st == 1:
+        u16 = raw.view(np.uint16)[:, :dim].astype(np.uint32)
+        return (u16 << 16).view(np.float32)
+    dpad = (dim + 15) // 16 * 16
+    scale = raw[:, dpad:dpad + 4].copy().view(np.float32)[:, 0]
+    vals = E4M3[raw[:, :dim]]
+    return (vals * scale[:, None]).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Early-exit network: training kernels (device) and checks (host)
+# ---------------------------------------------------------------------------
+
+def mlp_init(seed=0):
+    """He-style initial FP32 parameters in the SONG_MLP_PARAMS layout."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(MLP_PARAMS, dtype=np.float32)
+    p[0:160] = rng.standard_normal(160) * np.sqrt(2.0 / 5)
+    p[192:1216] = rng.standard_normal(1024) * np.sqrt(2.0 / 32)
+    p[1248:1280] = rng.standard_normal(32) * np.sqrt(1.0 / 32)
+    return p
+
+
+def mlp_grad(x, y, params, w=None):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    w = None if w is None else np.ascontiguousarray(w, np.float32)
+    params = np.ascontiguousarray(params, np.float32)
+    g = np.empty(MLP_PARAMS, np.float32)
+    loss = np.zeros(1, np.float32)
+    _check(load_library().song_mlp_grad(_ptr(x), _ptr(y), _ptr(w), x.shape[0], _ptr(params), _ptr(g), _ptr(loss)))
+    return g, float(loss[0])
+
+
+def mlp_forward(x, params):
+    x = np.ascontiguousarray(x, np.float32)
+    params = np.ascontiguousarray(params, np.float32)
+    out = np.empty(x.shape[0], np.float32)
+    _check(load_library().song_mlp_forward(_ptr(x), x.shape[0], _ptr(params), _ptr(out)))
+    return out
+
+
+def mlp_train_device(x_ptr, y_ptr, w_ptr, n, perm_ptr, epochs, batch, lr, params_ptr, loss_ptr=None, stream=None):
+    """song_mlp_train_device on raw device pointers."""
+    v = lambda a: ctypes.c_void_p(a) if a else None
+    _check(load_library().song_mlp_train_device(v(x_ptr), v(y_ptr), v(w_ptr), int(n), v(perm_ptr), int(epochs),
+                                                int(batch), float(lr), v(params_ptr), v(loss_ptr), v(stream)))

@@ -1,6 +1,8 @@
 // capi.cu -- the extern "C" boundary (include/song_gb300.h): resident index,
 // search entry points with host or device buffers, and the one-shot form with
 // the reference's argument list.
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -88,10 +90,10 @@ int grow(T **p, size_t *cap, size_t need, uint64_t *acct) {
 
 void release(song_index *ix) {
   if (!ix) return;
+  if (ix->d_rows_f32 && static_cast<void *>(ix->d_rows_f32) != ix->d_rows) cudaFree(ix->d_rows_f32);
   cudaFree(ix->d_rows);
   cudaFree(ix->d_adj);
-  cudaFree(ix->d_scale);
-  if (ix->d_rows_f32 && ix->d_rows_f32 != ix->d_rows) cudaFree(ix->d_rows_f32);
+  cudaFree(ix->d_mlp);
   cudaFree(ix->d_counter);
   cudaFree(ix->d_error);
   cudaFree(ix->d_q);
@@ -113,6 +115,7 @@ int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_
   c.evals = d_evals;
   c.counter = ix->d_counter;
   c.error = ix->d_error;
+  song::apply_index_settings(ix, c);
   SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
   int e = song::launch_search(ix->dx, c, s);
   if (e == -1) return fail(SONG_ERR_ARG, "unsupported search shape");
@@ -120,6 +123,56 @@ int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_
   return SONG_OK;
 }
 
+
+// BF16 rows: round-to-nearest-even conversion of every element, zero padding.
+__global__ void to_bf16_kernel(const float *in, uint32_t in_row_floats, uint64_t n, int dim, int dpad,
+                               __nv_bfloat16 *out) {
+  const uint64_t total = n * static_cast<uint64_t>(dpad);
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t r = i / dpad;
+    const int j = static_cast<int>(i - r * dpad);
+    out[i] = __float2bfloat16_rn(j < dim ? in[r * in_row_floats + j] : 0.0f);
+  }
+}
+
+// FP8 rows, one warp per row: scale = max|x| / 448 (the largest finite E4M3
+// value; 1 for a zero row), elements x / scale converted with saturation to
+// E4M3, the scale stored as a float at scale_off.
+__global__ void to_fp8_kernel(const float *in, uint32_t in_row_floats, uint64_t n, int dim,
+                              uint8_t *out, uint32_t out_row_bytes, uint32_t scale_off) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t r = warp; r < n; r += nwarps) {
+    const float *x = in + r * in_row_floats;
+    float amax = 0.0f;
+    for (int j = lane; j < dim; j += 32) amax = fmaxf(amax, fabsf(x[j]));
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    const float scale = amax > 0.0f ? amax / 448.0f : 1.0f;
+    uint8_t *y = out + r * out_row_bytes;
+    for (int j = lane; j < static_cast<int>(scale_off); j += 32)
+      y[j] = j < dim ? static_cast<uint8_t>(__nv_cvt_float_to_fp8(x[j] / scale, __NV_SATFINITE, __NV_E4M3)) : 0;
+    for (int j = static_cast<int>(scale_off) + lane; j < static_cast<int>(out_row_bytes); j += 32) y[j] = 0;
+    __syncwarp();
+    if (lane == 0) *reinterpret_cast<float *>(y + scale_off) = scale;
+  }
+}
+
+}  // namespace
+
+namespace song {
+void apply_index_settings(const song_index *ix, SearchCall &c) {
+  c.rerank = ix->dx.storage == SONG_STORAGE_F32 ? 0 : (ix->rerank < 0 ? c.pq : ix->rerank);
+  c.mlp = ix->d_mlp;
+  c.exit_threshold = ix->exit_threshold;
+  c.exit_min_hops = ix->exit_min_hops;
+  c.exit_every = ix->exit_every;
+  c.exit_max_hops = ix->max_hops;
+}
+}  // namespace song
+
+namespace {
 }  // namespace
 
 extern "C" {
@@ -149,7 +202,7 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   if (shift < 1 || shift > SONG_MAX_SHIFT)
     return fail(SONG_ERR_ARG, "shift must be in [1, %d]", SONG_MAX_SHIFT);
   if (metric < SONG_METRIC_L2 || metric > SONG_METRIC_COS) return fail(SONG_ERR_ARG, "bad metric");
-  if (storage != SONG_STORAGE_F32) return fail(SONG_ERR_ARG, "storage %d not available", storage);
+  if (storage < SONG_STORAGE_F32 || storage > SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "bad storage %d", storage);
 
   // The reference reads degree and ids unchecked (warp_astar_accelerator.h:212-214);
   // a malformed row would make it read out of bounds, so reject it here.
@@ -182,10 +235,19 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   dx.shift = shift;
   dx.metric = metric;
   dx.storage = storage;
-  dx.dpad = (dim + 3) / 4 * 4;
-  dx.row_bytes = static_cast<uint32_t>(dx.dpad) * 4u;
-  dx.f32_row_bytes = dx.row_bytes;
-
+  const int dpad4 = (dim + 3) / 4 * 4;
+  dx.f32_row_bytes = static_cast<uint32_t>(dpad4) * 4u;
+  if (storage == SONG_STORAGE_F32) {
+    dx.dpad = dpad4;
+    dx.row_bytes = dx.f32_row_bytes;
+  } else if (storage == SONG_STORAGE_BF16) {
+    dx.dpad = (dim + 7) / 8 * 8;
+    dx.row_bytes = static_cast<uint32_t>(dx.dpad) * 2u;
+  } else {
+    dx.dpad = (dim + 15) / 16 * 16;
+    dx.scale_off = static_cast<uint32_t>(dx.dpad);
+    dx.row_bytes = dx.scale_off + 16u;
+  }
   auto bail = [&](int code) {
     release(ix);
     return code;
@@ -199,12 +261,29 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
                        #call, cudaGetErrorString(e)));                                      \
   } while (0)
   SONG_CUDA_IX(cudaStreamCreateWithFlags(&ix->stream, cudaStreamNonBlocking));
-  const size_t rows_bytes = static_cast<size_t>(n) * dx.row_bytes;
-  SONG_CUDA_IX(cudaMalloc(&ix->d_rows, rows_bytes));
-  ix->device_bytes += rows_bytes;
-  SONG_CUDA_IX(cudaMemsetAsync(ix->d_rows, 0, rows_bytes, ix->stream));
-  SONG_CUDA_IX(cudaMemcpy2DAsync(ix->d_rows, dx.row_bytes, data, sizeof(float) * dim,
+  const size_t f32_bytes = static_cast<size_t>(n) * dx.f32_row_bytes;
+  SONG_CUDA_IX(cudaMalloc(reinterpret_cast<void **>(&ix->d_rows_f32), f32_bytes));
+  ix->device_bytes += f32_bytes;
+  SONG_CUDA_IX(cudaMemsetAsync(ix->d_rows_f32, 0, f32_bytes, ix->stream));
+  SONG_CUDA_IX(cudaMemcpy2DAsync(ix->d_rows_f32, dx.f32_row_bytes, data, sizeof(float) * dim,
                                  sizeof(float) * dim, n, cudaMemcpyHostToDevice, ix->stream));
+  if (storage == SONG_STORAGE_F32) {
+    ix->d_rows = ix->d_rows_f32;
+  } else {
+    // Low-precision rows for the search; the FP32 rows stay for the re-rank.
+    const size_t rows_bytes = static_cast<size_t>(n) * dx.row_bytes;
+    SONG_CUDA_IX(cudaMalloc(&ix->d_rows, rows_bytes));
+    ix->device_bytes += rows_bytes;
+    const uint32_t in_floats = dx.f32_row_bytes / 4u;
+    if (storage == SONG_STORAGE_BF16)
+      to_bf16_kernel<<<4 * 152, 256, 0, ix->stream>>>(ix->d_rows_f32, in_floats, n, dim, dx.dpad,
+                                                      static_cast<__nv_bfloat16 *>(ix->d_rows));
+    else
+      to_fp8_kernel<<<4 * 152, 256, 0, ix->stream>>>(ix->d_rows_f32, in_floats, n, dim,
+                                                     static_cast<uint8_t *>(ix->d_rows), dx.row_bytes,
+                                                     dx.scale_off);
+    SONG_CUDA_IX(cudaGetLastError());
+  }
   SONG_CUDA_IX(cudaMalloc(&ix->d_adj, slots * sizeof(uint32_t)));
   ix->device_bytes += slots * sizeof(uint32_t);
   SONG_CUDA_IX(cudaMemcpyAsync(ix->d_adj, adj.data(), slots * sizeof(uint32_t),
@@ -216,7 +295,7 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   SONG_CUDA_IX(cudaStreamSynchronize(ix->stream));
 #undef SONG_CUDA_IX
   dx.rows = ix->d_rows;
-  dx.rows_f32 = static_cast<const float *>(ix->d_rows);
+  dx.rows_f32 = ix->d_rows_f32;
   dx.adj = ix->d_adj;
   *out = ix;
   return SONG_OK;
@@ -344,6 +423,103 @@ int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_ou
   cudaFree(d_ids);
   cudaFree(d_out);
   if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "debug fixhash: %s", cudaGetErrorString(e));
+  return SONG_OK;
+}
+
+
+int song_index_set_rerank(song_index *ix, int rerank) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (rerank < -1 || rerank > SONG_MAX_PQ) return fail(SONG_ERR_ARG, "rerank must be in [-1, %d]", SONG_MAX_PQ);
+  ix->rerank = rerank;
+  return SONG_OK;
+}
+
+int song_index_set_early_exit(song_index *ix, const float *weights, float threshold, int min_hops,
+                              int every) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  if (!weights) {
+    cudaFree(ix->d_mlp);
+    ix->d_mlp = nullptr;
+    return SONG_OK;
+  }
+  if (every < 1 || min_hops < 0) return fail(SONG_ERR_ARG, "every must be >= 1 and min_hops >= 0");
+  if (ix->dx.storage == SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "early exit is built for F32 and BF16 storage");
+  std::vector<__nv_bfloat16> w(SONG_MLP_PARAMS);
+  for (int i = 0; i < SONG_MLP_PARAMS; ++i) w[i] = __float2bfloat16_rn(weights[i]);
+  if (!ix->d_mlp) {
+    SONG_CUDA(cudaMalloc(reinterpret_cast<void **>(&ix->d_mlp), sizeof(__nv_bfloat16) * SONG_MLP_PARAMS));
+    ix->device_bytes += sizeof(__nv_bfloat16) * SONG_MLP_PARAMS;
+  }
+  SONG_CUDA(cudaMemcpy(ix->d_mlp, w.data(), sizeof(__nv_bfloat16) * SONG_MLP_PARAMS, cudaMemcpyHostToDevice));
+  ix->exit_threshold = threshold;
+  ix->exit_min_hops = min_hops;
+  ix->exit_every = every;
+  return SONG_OK;
+}
+
+int song_index_set_hop_limit(song_index *ix, int max_hops) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (max_hops < 0) return fail(SONG_ERR_ARG, "max_hops must be >= 0");
+  if (max_hops > 0 && ix->dx.storage == SONG_STORAGE_FP8)
+    return fail(SONG_ERR_ARG, "the hop limit is built for F32 and BF16 storage");
+  ix->max_hops = max_hops;
+  return SONG_OK;
+}
+
+int song_search_trace_device(song_index *ix, const float *d_queries, int nq, int pq, int k,
+                             int trace_hops, float *d_trace, int32_t *d_final, uint64_t *d_out,
+                             int32_t *d_hops, int32_t *d_evals, void *stream) {
+  g_last_error.clear();
+  int rc = check_search_args(ix, nq, pq, k);
+  if (rc) return rc;
+  if (nq == 0) return SONG_OK;
+  if (!d_queries || !d_out || !d_trace || !d_final || trace_hops < 1)
+    return fail(SONG_ERR_ARG, "null buffer or trace_hops < 1");
+  if (ix->dx.storage == SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "tracing is built for F32 and BF16 storage");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  song::SearchCall c;
+  c.queries = d_queries;
+  c.nq = nq;
+  c.pq = pq;
+  c.k = k;
+  c.out = d_out;
+  c.hops = d_hops;
+  c.evals = d_evals;
+  c.counter = ix->d_counter;
+  c.error = ix->d_error;
+  song::apply_index_settings(ix, c);
+  c.mlp = nullptr;  // traces record the full search
+  c.exit_max_hops = 0;
+  c.trace = d_trace;
+  c.trace_hops = trace_hops;
+  c.trace_final = d_final;
+  SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
+  int e = song::launch_search(ix->dx, c, s);
+  if (e == -1) return fail(SONG_ERR_ARG, "unsupported search shape");
+  if (e != 0) return fail(SONG_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)e));
+  return SONG_OK;
+}
+
+int song_index_rows(const song_index *ix, uint64_t first, uint64_t count, void *out, size_t out_bytes,
+                    int *row_bytes) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (row_bytes) *row_bytes = static_cast<int>(ix->dx.row_bytes);
+  if (!out) return SONG_OK;
+  const size_t need = static_cast<size_t>(count) * ix->dx.row_bytes;
+  if (first > ix->dx.n || count > ix->dx.n - first || out_bytes < need)
+    return fail(SONG_ERR_ARG, "rows out of range or buffer too small");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  SONG_CUDA(cudaMemcpy(out, static_cast<const uint8_t *>(ix->d_rows) + first * ix->dx.row_bytes, need,
+                       cudaMemcpyDeviceToHost));
   return SONG_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace song {
@@ -16,7 +17,7 @@ struct DeviceIndex {
   int dpad = 0;             // elements per stored row (row_bytes / element size)
   uint32_t row_bytes = 0;   // bytes per stored row, a multiple of 16
   const void *rows = nullptr;        // n rows of row_bytes
-  const float *row_scale = nullptr;  // FP8: one scale per row
+  uint32_t scale_off = 0;            // FP8: byte offset of the per-row float scale
   const float *rows_f32 = nullptr;   // FP32 rows (rerank; == rows for F32 storage)
   uint32_t f32_row_bytes = 0;
   const uint32_t *adj = nullptr;     // n << shift uint32: slot 0 = degree
@@ -32,6 +33,15 @@ struct SearchCall {
   int32_t *evals = nullptr;        // nq or null
   uint32_t *counter = nullptr;     // one uint32 of device scratch (work counter)
   int32_t *error = nullptr;        // one int32 device error flag
+  int rerank = 0;                  // low-precision storage: FP32 re-rank of the best `rerank`
+  const __nv_bfloat16 *mlp = nullptr;  // early-exit network (device, BF16) or null
+  float exit_threshold = 0.0f;     // stop when the network's logit >= this
+  int exit_min_hops = 0;
+  int exit_every = 1;
+  int exit_max_hops = 0;           // > 0: fixed hop budget (comparison heuristic)
+  float *trace = nullptr;          // per-hop features, nq x trace_hops x 6, or null
+  int trace_hops = 0;
+  int32_t *trace_final = nullptr;  // nq x 2: final top-k version, hops traced
 };
 
 // Launch the plain search.  Returns a cudaError_t-compatible code (0 ok) or
@@ -53,6 +63,8 @@ namespace song {
 int fail(int code, const char *fmt, ...);
 void clear_error();
 int check_search_args(const song_index *ix, int nq, int pq, int k);
+// Copies the index's search settings (re-rank count, early-exit network) into c.
+void apply_index_settings(const song_index *ix, SearchCall &c);
 }  // namespace song
 
 // The opaque handle of include/song_gb300.h.
@@ -61,8 +73,13 @@ struct song_index {
   song::DeviceIndex dx;
   void *d_rows = nullptr;
   uint32_t *d_adj = nullptr;
-  float *d_scale = nullptr;
   float *d_rows_f32 = nullptr;
+  int rerank = -1;                  // -1: all pq candidates (default), 0: none
+  __nv_bfloat16 *d_mlp = nullptr;   // early-exit network, null = off
+  float exit_threshold = 0.0f;
+  int exit_min_hops = 0;
+  int exit_every = 1;
+  int max_hops = 0;                 // fixed hop budget, 0 = off
   uint32_t *d_counter = nullptr;
   int32_t *d_error = nullptr;
   cudaStream_t stream = nullptr;

@@ -107,6 +107,7 @@ extern "C" int song_search_noalloc(song_index *ix, const float *queries, int nq,
       c.out = d_out;
       c.counter = counter;
       c.error = error;
+      song::apply_index_settings(ix, c);
       int le = song::launch_search(ix->dx, c, s);
       if (le == -1) rc = song::fail(SONG_ERR_ARG, "unsupported search shape");
       else e = static_cast<cudaError_t>(le);

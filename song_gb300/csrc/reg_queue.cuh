@@ -1,11 +1,20 @@
 // reg_queue.cuh -- a sorted array of (distance, id) keys held in the registers
-// of one warp, lane-blocked: lane l holds elements l*S .. l*S+S-1.  Capacity
-// 32*S.  Every operation is warp-uniform; dynamic positions are resolved with
-// unrolled compare/select over the S slots, so the array never leaves the
-// register file.  Replaces the reference's serial min-max heap (smmh2.h) and
-// binary heap (bin_heap.h): insert, pop-min and drop-max cost O(S) register
-// operations and one or two shuffles instead of O(log pq) dependent memory
-// accesses by one thread.
+// of one warp.  Replaces the reference's serial min-max heap (smmh2.h) and
+// binary heap (bin_heap.h).
+//
+// Layout: capacity C = 32*S positions, lane-blocked (lane l holds positions
+// l*S .. l*S+S-1 in v[0..S-1]), ascending, RIGHT-aligned: the n live keys sit
+// at positions C-n .. C-1 and every position left of them holds 0, a key
+// smaller than any real key (real keys carry order-preserving distance bits
+// >= 0x007fffff in their high word).  Consequences:
+//   * the maximum is always at position C-1 (lane 31, v[S-1]): O(1);
+//   * inserting without eviction moves the smaller keys one place left,
+//     inserting with eviction of the maximum moves the larger keys one place
+//     right; neither needs the insertion position, only per-slot compares
+//     against the new key and one shuffle for the lane boundary;
+//   * removing the minimum (position C-n) is the only operation that touches
+//     a dynamic position: one select pass over the S slots.
+// All operations are warp-uniform.
 #pragma once
 
 #include <cstdint>
@@ -16,57 +25,72 @@ namespace song {
 
 template <int S>
 struct RegQueue {
+  static constexpr int C = 32 * S;
   uint64_t v[S];
 
   __device__ __forceinline__ void clear() {
 #pragma unroll
-    for (int j = 0; j < S; ++j) v[j] = ~0ull;
+    for (int j = 0; j < S; ++j) v[j] = 0ull;
   }
 
-  // Element i (0 <= i < 32*S), broadcast to all lanes.
-  __device__ __forceinline__ uint64_t get(int i) const {
-    const int l = i / S, s = i - l * S;
-    uint64_t x = v[0];
+  // Largest live key (0 when empty).
+  __device__ __forceinline__ uint64_t max() const { return __shfl_sync(FULL, v[S - 1], 31); }
+
+  // Key at position pos (broadcast).
+  // (Selections compare the full position, lane*S + j, rather than a slot
+  // index: written as "slot == r" the compiler turns the loop into a dynamic
+  // array index and moves the array to local memory.)
+  __device__ __forceinline__ uint64_t at(int pos, int lane) const {
+    uint64_t x = 0;
 #pragma unroll
-    for (int j = 1; j < S; ++j)
-      if (j == s) x = v[j];
-    return __shfl_sync(FULL, x, l);
+    for (int j = 0; j < S; ++j) x = (lane * S + j) == pos ? v[j] : x;
+    return __shfl_sync(FULL, x, pos / S);
   }
 
-  // Number of the first n elements that are < key (= insertion position).
-  __device__ __forceinline__ int lower_bound(uint64_t key, int n, int lane) const {
-    int c = 0;
+  // Insert, n -> n + 1 (requires n < C): keys below `key` move one place left.
+  __device__ __forceinline__ void insert_grow(uint64_t key, int lane) {
+    uint64_t nxt = __shfl_down_sync(FULL, v[0], 1);
+    if (lane == 31) nxt = ~0ull;
 #pragma unroll
-    for (int j = 0; j < S; ++j) c += (lane * S + j < n && v[j] < key) ? 1 : 0;
-    return static_cast<int>(__reduce_add_sync(FULL, static_cast<unsigned>(c)));
-  }
-
-  // Insert key at position p; elements p.. move up one place (the last one of
-  // a full array falls off).
-  __device__ __forceinline__ void insert_at(int p, uint64_t key, int lane) {
-    const uint64_t carry = __shfl_up_sync(FULL, v[S - 1], 1);
-#pragma unroll
-    for (int j = S - 1; j >= 0; --j) {
-      const int i = lane * S + j;
-      const uint64_t prev = j > 0 ? v[j - 1] : carry;
-      v[j] = i < p ? v[j] : (i == p ? key : prev);
+    for (int j = 0; j < S; ++j) {
+      const uint64_t right = j + 1 < S ? v[j + 1] : nxt;
+      v[j] = right < key ? right : (v[j] < key ? key : v[j]);
     }
   }
 
-  __device__ __forceinline__ int insert(uint64_t key, int &n, int lane) {
-    const int p = lower_bound(key, n, lane);
-    insert_at(p, key, lane);
-    ++n;
-    return p;
+  // Insert and drop the maximum, n unchanged: keys not below `key` move one
+  // place right and the old maximum falls off.  If key >= the maximum nothing
+  // changes (the key itself is dropped).
+  __device__ __forceinline__ void insert_evict(uint64_t key, int lane) {
+    uint64_t prv = __shfl_up_sync(FULL, v[S - 1], 1);
+    if (lane == 0) prv = 0ull;
+#pragma unroll
+    for (int j = S - 1; j >= 0; --j) {
+      const uint64_t left = j > 0 ? v[j - 1] : prv;
+      v[j] = v[j] < key ? v[j] : (left < key ? key : left);
+    }
   }
 
-  // Remove element 0; everything moves down one place.
-  __device__ __forceinline__ void pop_front(int lane) {
-    const uint64_t nxt = __shfl_down_sync(FULL, v[0], 1);
+  // Remove the minimum of n >= 1 live keys; returns it, and the new minimum
+  // in *next (~0 if none is left).
+  __device__ __forceinline__ uint64_t pop_min(int n, int lane, uint64_t *next) {
+    const int pos = C - n;
+    uint64_t x = 0, y = ~0ull;
 #pragma unroll
-    for (int j = 0; j < S - 1; ++j) v[j] = v[j + 1];
-    v[S - 1] = lane == 31 ? ~0ull : nxt;
+    for (int j = 0; j < S; ++j) {
+      const int q = lane * S + j;
+      x = q == pos ? v[j] : x;
+      y = q == pos + 1 ? v[j] : y;
+      v[j] = q == pos ? 0ull : v[j];
+    }
+    const uint64_t m = __shfl_sync(FULL, x, pos / S);
+    *next = n > 1 ? __shfl_sync(FULL, y, (pos + 1) / S) : ~0ull;
+    return m;
   }
+
+  // Key of rank i (0 = smallest) among n live keys, for the output: lane l's
+  // slot j holds rank l*S + j - (C - n).
+  __device__ __forceinline__ int rank_of(int j, int n, int lane) const { return lane * S + j - (C - n); }
 };
 
 }  // namespace song

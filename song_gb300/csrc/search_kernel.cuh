@@ -1,0 +1,521 @@
+// search_kernel.cuh -- the batched best-first graph search kernel for sm_103a.
+//
+// It computes what warp_independent_search_kernel computes
+// (warp_astar_accelerator.h:41-341): for each query, a best-first walk from
+// vertex 0 over the fixed-degree graph with a candidate queue bounded at pq,
+// a top-pq list of expanded vertices, a visited hash over queue and list, the
+// select-insert rule (skip a candidate when the queue is full and its maximum
+// is closer) and the finish rule (stop when the list is full and its maximum
+// is <= the vertex just popped).  With FP32 storage the distances are the
+// reference's bit for bit: lane l sums dims l, l+32, ... with fused
+// multiply-add and the 32 partial sums meet in the xor butterfly 16,8,4,2,1.
+//
+// GB300 design:
+//  * persistent warps pull queries from a work counter; warps never wait for
+//    one another (the only block barrier is the model load at kernel start);
+//  * per-query state: query vector, visited hash (the reference's FixHash,
+//    8*pq slots) and a two-buffer staging ring in the warp's shared memory;
+//    candidate queue and top-pq list in registers (reg_queue.cuh);
+//  * each hop's unvisited neighbour rows are gathered with 1-D bulk async
+//    copies (cp.async.bulk, mbarrier transaction counts) into the ring, two
+//    chunks in flight, and read back in the reference's lane order;
+//  * the next hop's adjacency row is loaded as soon as the next pop is known.
+//
+// Template parameters: METRIC (0 L2, 1 IP, 2 COS), STORAGE (0 F32, 1 BF16,
+// 2 FP8-E4M3 with a per-row scale), H (rows per staging buffer), S (register
+// queue segment, capacity 32*S >= pq+1), LEARNED (per-hop features: trace
+// capture and/or the early-exit network).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "internal.h"
+#include "reg_queue.cuh"
+
+namespace song {
+
+constexpr int MAX_WARPS_PER_BLOCK = 4;
+constexpr int MLP_IN = 5, MLP_H = 32;
+// FP32 parameters of the early-exit network, in this order.
+constexpr int MLP_W1 = 0;                        // [MLP_H][MLP_IN]
+constexpr int MLP_B1 = MLP_W1 + MLP_H * MLP_IN;  // [MLP_H]
+constexpr int MLP_W2 = MLP_B1 + MLP_H;           // [MLP_H][MLP_H]
+constexpr int MLP_B2 = MLP_W2 + MLP_H * MLP_H;   // [MLP_H]
+constexpr int MLP_W3 = MLP_B2 + MLP_H;           // [MLP_H]
+constexpr int MLP_B3 = MLP_W3 + MLP_H;           // [1]
+constexpr int MLP_NPARAM = MLP_B3 + 1;
+constexpr int TRACE_FIELDS = 6;  // 5 features + top-k version
+
+struct Params {
+  const uint8_t *rows;
+  uint32_t row_bytes;
+  uint32_t scale_off;  // FP8: byte offset of the row's float scale
+  const float *rows_f32;
+  uint32_t f32_row_bytes;
+  int rerank;  // final candidates re-ranked with FP32 distances (low-precision storage)
+  const uint32_t *adj;
+  int shift;
+  int dim;
+  const float *queries;
+  int nq, pq, k;
+  uint64_t *out;
+  int32_t *hops;
+  int32_t *evals;
+  uint32_t *counter;
+  int32_t *error;
+  uint32_t warp_bytes;
+  uint32_t off_mbar, off_cand, off_q, off_hash;
+  int cap;
+  uint64_t magic;
+  // learned variant
+  const __nv_bfloat16 *mlp;  // MLP_NPARAM weights (BF16), null = no early exit
+  float exit_threshold;
+  int exit_min_hops;
+  int exit_every;
+  int exit_max_hops;      // > 0: stop after this many hops (fixed-budget heuristic)
+  float *trace;           // [nq][trace_hops][TRACE_FIELDS] or null
+  int trace_hops;
+  int32_t *trace_final;   // [nq]: final top-k version, hops traced
+};
+
+template <int METRIC>
+__device__ __forceinline__ float finish_distance(float t, float len) {
+  if (METRIC == 0) return t;
+  if (METRIC == 1) return -t;
+  // warp_astar_accelerator.h:275-281: sign * tmp * tmp / len in float.
+  if (len != 0.0f) {
+    float sign = t < 0.0f ? 1.0f : -1.0f;
+    return __fdiv_rn(__fmul_rn(__fmul_rn(sign, t), t), len);
+  }
+  return 0.0f;
+}
+
+// Element j of a staged row as float.  FP8 elements are decoded and scaled
+// (x = e4m3(y) * scale, rounded to float), so a low-precision search equals
+// an FP32 search over the dequantised vectors.
+template <int STORAGE>
+__device__ __forceinline__ float load_elem(const uint8_t *row, int j, float scale) {
+  if (STORAGE == 0) return reinterpret_cast<const float *>(row)[j];
+  if (STORAGE == 1) return __bfloat162float(reinterpret_cast<const __nv_bfloat16 *>(row)[j]);
+  const __half_raw h = __nv_cvt_fp8_to_halfraw(static_cast<__nv_fp8_storage_t>(row[j]), __NV_E4M3);
+  return __fmul_rn(__half2float(__half(h)), scale);
+}
+
+// Distances of candidates 0..m-1 (candidate c's id in lane c); candidate c's
+// distance is returned in lane c.  False if a bulk copy never completed.
+template <int METRIC, int STORAGE, int H>
+__device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage, uint64_t *mbar,
+                                                 uint32_t &ph0, uint32_t &ph1, const float *qv,
+                                                 int m, uint32_t cid, float &out, int lane) {
+  const int nchunks = (m + H - 1) / H;
+  const uint32_t rb = p.row_bytes;
+  auto issue = [&](int c) {
+    const int b = c & 1;
+    const int first = c * H;
+    const int cnt = min(H, m - first);
+    // The buffer was last read through the generic proxy; order those reads
+    // before the async-proxy writes of the copies issued below.
+    fence_proxy_async();
+    if (lane == 0) mbar_arrive_expect_tx(&mbar[b], static_cast<uint32_t>(cnt) * rb);
+    __syncwarp();
+    const uint32_t id = __shfl_sync(FULL, cid, (first + lane) & 31);
+    if (lane < cnt)
+      bulk_g2s(stage + static_cast<size_t>(b * H + lane) * rb,
+               p.rows + static_cast<uint64_t>(id) * rb, rb, &mbar[b]);
+  };
+  if (nchunks > 0) issue(0);
+  if (nchunks > 1) issue(1);
+  out = 0.0f;
+  for (int c = 0; c < nchunks; ++c) {
+    const int b = c & 1;
+    uint32_t &ph = b ? ph1 : ph0;
+    if (!mbar_wait(&mbar[b], ph)) return false;
+    ph ^= 1u;
+    const int first = c * H;
+    const int cnt = min(H, m - first);
+    const uint8_t *buf = stage + static_cast<size_t>(b * H) * rb;
+    float acc[H], len[H];
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      acc[i] = 0.0f;
+      len[i] = 0.0f;
+      if (i < cnt) {
+        const uint8_t *x = buf + static_cast<size_t>(i) * rb;
+        const float scale = STORAGE == 2 ? *reinterpret_cast<const float *>(x + p.scale_off) : 1.0f;
+        for (int j = lane; j < p.dim; j += 32) {
+          const float qj = qv[j];
+          const float xj = load_elem<STORAGE>(x, j, scale);
+          if (METRIC == 0) {
+            const float d = __fsub_rn(qj, xj);
+            acc[i] = __fmaf_rn(d, d, acc[i]);
+          } else {
+            acc[i] = __fmaf_rn(qj, xj, acc[i]);
+            if (METRIC == 2) len[i] = __fmaf_rn(xj, xj, len[i]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int i = 0; i < H; ++i) {
+        acc[i] = __fadd_rn(acc[i], __shfl_xor_sync(FULL, acc[i], o));
+        if (METRIC == 2) len[i] = __fadd_rn(len[i], __shfl_xor_sync(FULL, len[i], o));
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < H; ++i)
+      if (i < cnt && lane == first + i) out = finish_distance<METRIC>(acc[i], len[i]);
+    __syncwarp();
+    if (c + 2 < nchunks) issue(c + 2);
+  }
+  return true;
+}
+
+// FP32 distances (reference arithmetic) of up to 4 rows loaded straight from
+// global memory, lane-strided and coalesced; result i in every lane.
+template <int METRIC>
+__device__ __forceinline__ void fp32_distances4(const Params &p, const float *qv,
+                                                const uint32_t ids[4], int cnt, float d[4],
+                                                int lane) {
+  float acc[4], len[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    acc[i] = 0.0f;
+    len[i] = 0.0f;
+  }
+  for (int j = lane; j < p.dim; j += 32) {
+    const float qj = qv[j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i < cnt) {
+        const float *row = reinterpret_cast<const float *>(
+            reinterpret_cast<const uint8_t *>(p.rows_f32) + static_cast<uint64_t>(ids[i]) * p.f32_row_bytes);
+        const float xj = __ldg(row + j);
+        if (METRIC == 0) {
+          const float dd = __fsub_rn(qj, xj);
+          acc[i] = __fmaf_rn(dd, dd, acc[i]);
+        } else {
+          acc[i] = __fmaf_rn(qj, xj, acc[i]);
+          if (METRIC == 2) len[i] = __fmaf_rn(xj, xj, len[i]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      acc[i] = __fadd_rn(acc[i], __shfl_xor_sync(FULL, acc[i], o));
+      if (METRIC == 2) len[i] = __fadd_rn(len[i], __shfl_xor_sync(FULL, len[i], o));
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) d[i] = finish_distance<METRIC>(acc[i], len[i]);
+}
+
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t y = __shfl_xor_sync(FULL, x, o);
+    x = y < x ? y : x;
+  }
+  return x;
+}
+
+__device__ __forceinline__ float key_float(uint64_t k) {
+  const uint32_t b = key_dist(k);
+  return __uint_as_float((b & 0x80000000u) ? (b & 0x7fffffffu) : ~b);
+}
+
+// Early-exit network, warp-parallel: lane j owns hidden unit j of both layers.
+// BF16 weights in shared memory, FP32 arithmetic.  Returns the logit.
+__device__ __forceinline__ float mlp_logit(const __nv_bfloat16 *w, const float f[MLP_IN], int lane) {
+  float h1 = __bfloat162float(w[MLP_B1 + lane]);
+#pragma unroll
+  for (int i = 0; i < MLP_IN; ++i) h1 = __fmaf_rn(__bfloat162float(w[MLP_W1 + lane * MLP_IN + i]), f[i], h1);
+  h1 = fmaxf(h1, 0.0f);
+  float h2 = __bfloat162float(w[MLP_B2 + lane]);
+#pragma unroll
+  for (int i = 0; i < MLP_H; ++i)
+    h2 = __fmaf_rn(__bfloat162float(w[MLP_W2 + lane * MLP_H + i]), __shfl_sync(FULL, h1, i), h2);
+  h2 = fmaxf(h2, 0.0f);
+  float z = __fmul_rn(__bfloat162float(w[MLP_W3 + lane]), h2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) z = __fadd_rn(z, __shfl_xor_sync(FULL, z, o));
+  return __fadd_rn(z, __bfloat162float(w[MLP_B3]));
+}
+
+template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
+__global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(const Params p) {
+  extern __shared__ __align__(128) uint8_t smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  uint8_t *ws = smem_raw + static_cast<size_t>(wib) * p.warp_bytes;
+  uint8_t *stage = ws;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + p.off_mbar);
+  uint32_t *cbuf = reinterpret_cast<uint32_t *>(ws + p.off_cand);
+  float *qv = reinterpret_cast<float *>(ws + p.off_q);
+  VisitedHash vh{reinterpret_cast<int32_t *>(ws + p.off_hash), p.cap, p.magic};
+  RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
+  constexpr int C = RegQueue<S>::C;
+
+  __nv_bfloat16 *wmlp = reinterpret_cast<__nv_bfloat16 *>(smem_raw + static_cast<size_t>(nwarps) * p.warp_bytes);
+  if (LEARNED) {
+    if (p.mlp)
+      for (int i = threadIdx.x; i < MLP_NPARAM; i += blockDim.x) wmlp[i] = p.mlp[i];
+    __syncthreads();
+  }
+
+  if (lane == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  uint32_t ph0 = 0, ph1 = 0;
+  const int nslots = 1 << p.shift;
+
+  for (;;) {
+    uint32_t qid = 0;
+    if (lane == 0) qid = atomicAdd(p.counter, 1u);
+    qid = __shfl_sync(FULL, qid, 0);
+    if (qid >= static_cast<uint32_t>(p.nq)) break;
+
+    const float *qsrc = p.queries + static_cast<size_t>(qid) * p.dim;
+    for (int j = lane; j < p.dim; j += 32) qv[j] = qsrc[j];
+    vh.clear(lane);
+    // Adjacency row of vertex 0, the first vertex popped.
+    uint32_t next_id = 0;
+    uint32_t a_next = lane < nslots ? __ldg(p.adj + lane) : 0u;
+
+    // warp_astar_accelerator.h:115-176: distance to vertex 0, queue = {0}.
+    float cd;
+    if (!gather_distances<METRIC, STORAGE, H>(p, stage, mbar, ph0, ph1, qv, 1, 0u, cd, lane)) {
+      if (lane == 0) atomicOr(p.error, 1);
+      return;
+    }
+    const float d0 = __shfl_sync(FULL, cd, 0);
+    int qn = 0, tn = 0;
+    Q.clear();
+    T.clear();
+    Q.insert_grow(make_key(d0, 0u), lane);
+    qn = 1;
+    vh.add(0u, lane);
+    int hops = 0, evals = 1;
+    int version = 0;  // number of changes of the top-k set (LEARNED)
+    float *trace = nullptr;
+    if (LEARNED && p.trace) trace = p.trace + static_cast<size_t>(qid) * p.trace_hops * TRACE_FIELDS;
+    const float dscale = 1.0f / (fabsf(d0) + 1e-30f);
+
+    while (qn > 0) {
+      // :186-193 pop the minimum, drop it from the visited hash.
+      uint64_t qh;  // queue minimum after the pop
+      const uint64_t now = Q.pop_min(qn, lane, &qh);
+      --qn;
+      const uint32_t now_id = key_id(now);
+      uint32_t a = a_next;
+      if (now_id != next_id)  // not taken: the prefetch predicts the pop exactly
+        a = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(now_id) << p.shift) + lane) : 0u;
+      vh.del(now_id, lane);
+      // :191 finish test (<=) against the list maximum.
+      if (tn == p.pq && key_dist(T.max()) <= key_dist(now)) break;
+      ++hops;
+      if (LEARNED) {  // does `now` enter the current top-k?
+        if (tn < p.k || now < T.at(C - tn + p.k - 1, lane)) ++version;
+      }
+      // :198-210 move it to the top-pq list (when full, `now` is below the
+      // list maximum, which is the one dropped).
+      if (tn < p.pq) {
+        T.insert_grow(now, lane);
+        ++tn;
+        vh.add(now_id, lane);
+      } else {
+        const uint64_t ev = T.max();
+        T.insert_evict(now, lane);
+        vh.add(now_id, lane);
+        vh.del(key_id(ev), lane);
+      }
+      // :211-224 neighbours not in the visited hash, in row order.
+      const int deg = static_cast<int>(__shfl_sync(FULL, a, 0));
+      const bool isnb = lane >= 1 && lane <= deg;
+      const bool fresh = isnb && !vh.test(a);
+      const unsigned fm = __ballot_sync(FULL, fresh);
+      const int m = __popc(fm);
+      if (fresh) cbuf[__popc(fm & lanemask_lt())] = a;
+      __syncwarp();
+      const uint32_t cid = lane < m ? cbuf[lane] : 0u;
+      // :237-287 distances.
+      if (!gather_distances<METRIC, STORAGE, H>(p, stage, mbar, ph0, ph1, qv, m, cid, cd, lane)) {
+        if (lane == 0) atomicOr(p.error, 1);
+        return;
+      }
+      evals += m;
+      // The next vertex popped is the smaller of the queue head and the best
+      // candidate (the select-insert rule can only reject candidates above a
+      // full queue's maximum); start loading its adjacency row now so that it
+      // arrives while the candidates are inserted.
+      const uint64_t ck = lane < m ? make_key(cd, cid) : ~0ull;
+      const uint64_t cmin = warp_min_u64(ck);
+      const uint64_t nk = cmin < qh ? cmin : qh;
+      if (nk != ~0ull) {
+        next_id = key_id(nk);
+        a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
+      }
+      // :297-322 select-insert in candidate order.
+      for (int c = 0; c < m; ++c) {
+        const float d = __shfl_sync(FULL, cd, c);
+        const uint32_t id = __shfl_sync(FULL, cid, c);
+        const uint64_t key = make_key(d, id);
+        if (qn < p.pq) {
+          Q.insert_grow(key, lane);
+          ++qn;
+          vh.add(id, lane);
+        } else {
+          const uint64_t qmax = Q.max();
+          if (key_dist(qmax) < key_dist(key)) continue;
+          // inserted, then the larger of the two leaves (:315-320)
+          const uint64_t ev = key < qmax ? qmax : key;
+          Q.insert_evict(key, lane);
+          vh.add(id, lane);
+          vh.del(key_id(ev), lane);
+        }
+      }
+      if (LEARNED) {
+        // Per-hop state: hop count, k-th and best distance, queue-head gap,
+        // distance evaluations; distances relative to the start distance.
+        const int kk = min(p.k, tn);
+        const float kth = key_float(T.at(C - tn + kk - 1, lane));
+        const float best = key_float(T.at(C - tn, lane));
+        const float head = nk != ~0ull ? key_float(nk) : kth;
+        float f[MLP_IN];
+        f[0] = __log2f(1.0f + static_cast<float>(hops)) * 0.1f;
+        f[1] = (kth - d0) * dscale;
+        f[2] = (best - d0) * dscale;
+        f[3] = (head - kth) * dscale;
+        f[4] = __log2f(1.0f + static_cast<float>(evals)) * 0.1f;
+        if (trace && hops <= p.trace_hops && lane < TRACE_FIELDS) {
+          float v = lane < MLP_IN ? f[0] : static_cast<float>(version);
+#pragma unroll
+          for (int i = 1; i < MLP_IN; ++i) v = lane == i ? f[i] : v;
+          trace[static_cast<size_t>(hops - 1) * TRACE_FIELDS + lane] = v;
+        }
+        if (p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= p.k) {
+          const float z = mlp_logit(wmlp, f, lane);
+          if (z >= p.exit_threshold) break;  // converged: stop before the pq budget
+        }
+        if (p.exit_max_hops > 0 && hops >= p.exit_max_hops) break;
+      }
+    }
+
+    uint64_t *o = p.out + static_cast<size_t>(qid) * p.k;
+    if (STORAGE != 0 && p.rerank > 0) {
+      // FP32 re-rank of the best `rerank` entries of the list, then the first k.
+      const int R = min(max(p.rerank, p.k), tn);
+      int rn = 0;
+      Q.clear();
+      for (int base = 0; base < R; base += 4) {
+        uint32_t ids[4];
+        const int cnt = min(4, R - base);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) ids[i] = i < cnt ? key_id(T.at(C - tn + base + i, lane)) : 0u;
+        float d[4];
+        fp32_distances4<METRIC>(p, qv, ids, cnt, d, lane);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (i < cnt) {
+            Q.insert_grow(make_key(d[i], ids[i]), lane);
+            ++rn;
+          }
+      }
+#pragma unroll
+      for (int j = 0; j < S; ++j) {
+        const int r = Q.rank_of(j, rn, lane);
+        if (r >= 0 && r < p.k) o[r] = static_cast<uint64_t>(key_id(Q.v[j]));
+      }
+      for (int i = rn + lane; i < p.k; i += 32) o[i] = ~0ull;
+    } else {
+      // :331-335 ascending ids; slots past the list length get UINT64_MAX.
+#pragma unroll
+      for (int j = 0; j < S; ++j) {
+        const int r = T.rank_of(j, tn, lane);
+        if (r >= 0 && r < p.k) o[r] = static_cast<uint64_t>(key_id(T.v[j]));
+      }
+      for (int i = tn + lane; i < p.k; i += 32) o[i] = ~0ull;
+    }
+    if (lane == 0) {
+      if (p.hops) p.hops[qid] = hops;
+      if (p.evals) p.evals[qid] = evals;
+      if (LEARNED && p.trace_final) {
+        p.trace_final[2 * qid] = version;
+        p.trace_final[2 * qid + 1] = min(hops, p.trace_hops);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launch helpers shared by the per-storage translation units.
+// ---------------------------------------------------------------------------
+
+// Launch shape per (kernel, bytes per block): warps per block in {4, 2, 1}
+// that keeps the most warps resident per SM (search.cu).
+int get_shape(const void *fn, uint32_t warp_bytes, uint32_t extra_bytes, int *wpb, int *grid_cap);
+
+template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
+int launch_kernel(const Params &p, cudaStream_t stream) {
+  auto kern = search_kernel<METRIC, STORAGE, H, S, LEARNED>;
+  const uint32_t extra = LEARNED ? static_cast<uint32_t>(MLP_NPARAM * sizeof(__nv_bfloat16) + 64) : 0u;
+  int wpb = 0, cap = 0;
+  int e = get_shape(reinterpret_cast<const void *>(kern), p.warp_bytes, extra, &wpb, &cap);
+  if (e != 0) return e;
+  const int want = (p.nq + wpb - 1) / wpb;
+  const int grid = want < cap ? (want > 0 ? want : 1) : cap;
+  cudaError_t ce = cudaMemsetAsync(p.counter, 0, sizeof(uint32_t), stream);
+  if (ce != cudaSuccess) return ce;
+  kern<<<grid, wpb * 32, static_cast<size_t>(p.warp_bytes) * wpb + extra, stream>>>(p);
+  return cudaGetLastError();
+}
+
+template <int METRIC, int STORAGE, int H, bool LEARNED>
+int launch_by_s(const Params &p, int S, cudaStream_t s) {
+  switch (S) {
+    case 1: return launch_kernel<METRIC, STORAGE, H, 1, LEARNED>(p, s);
+    case 2: return launch_kernel<METRIC, STORAGE, H, 2, LEARNED>(p, s);
+    case 4: return launch_kernel<METRIC, STORAGE, H, 4, LEARNED>(p, s);
+    case 8: return launch_kernel<METRIC, STORAGE, H, 8, LEARNED>(p, s);
+    case 16: return launch_kernel<METRIC, STORAGE, H, 16, LEARNED>(p, s);
+    case 32: return launch_kernel<METRIC, STORAGE, H, 32, LEARNED>(p, s);
+    default: return -1;
+  }
+}
+
+template <int STORAGE, bool LEARNED>
+int launch_storage(const Params &p, int metric, int H, int S, cudaStream_t s) {
+  switch (metric * 2 + (H == 4 ? 1 : 0)) {
+    case 0: return launch_by_s<0, STORAGE, 2, LEARNED>(p, S, s);
+    case 1: return launch_by_s<0, STORAGE, 4, LEARNED>(p, S, s);
+    case 2: return launch_by_s<1, STORAGE, 2, LEARNED>(p, S, s);
+    case 3: return launch_by_s<1, STORAGE, 4, LEARNED>(p, S, s);
+    case 4: return launch_by_s<2, STORAGE, 2, LEARNED>(p, S, s);
+    case 5: return launch_by_s<2, STORAGE, 4, LEARNED>(p, S, s);
+    default: return -1;
+  }
+}
+
+// One per translation unit (search_f32.cu, search_bf16.cu, search_fp8.cu,
+// search_learned.cu).
+int launch_f32(const Params &p, int metric, int H, int S, cudaStream_t s);
+int launch_bf16(const Params &p, int metric, int H, int S, cudaStream_t s);
+int launch_fp8(const Params &p, int metric, int H, int S, cudaStream_t s);
+int launch_learned(const Params &p, int storage, int metric, int H, int S, cudaStream_t s);
+
+}  // namespace song
