@@ -135,9 +135,10 @@ int song_index_rows(const song_index *index, uint64_t first, uint64_t count, voi
 
 /* Learned early exit (no counterpart in the reference).  A network
  * 5 -> 32 -> 32 -> 1 (ReLU) reads, after every `every`-th hop from hop
- * `min_hops` on, the query's state (log hop count, k-th and best list
- * distance and queue-head gap relative to the start distance, log distance
- * evaluations) and stops the search when its logit >= threshold; queries it
+ * `min_hops` on, the query's state (log hop count; the top-k spread and the
+ * queue-head gap relative to the progress span d0 - best, as signed logs;
+ * the progress (d0 - best) / (|d0| + |best|); log distance evaluations) and
+ * stops the search when its logit >= threshold; queries it
  * never trusts run the plain search to its finish rule.  weights: the
  * SONG_MLP_PARAMS FP32 parameters (W1[32][5], b1[32], W2[32][32], b2[32],
  * w3[32], b3), stored on the device in BF16; NULL switches the exit off.

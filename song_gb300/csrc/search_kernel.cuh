@@ -313,7 +313,6 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
     int version = 0;  // number of changes of the top-k set (LEARNED)
     float *trace = nullptr;
     if (LEARNED && p.trace) trace = p.trace + static_cast<size_t>(qid) * p.trace_hops * TRACE_FIELDS;
-    const float dscale = 1.0f / (fabsf(d0) + 1e-30f);
 
     while (qn > 0) {
       // :186-193 pop the minimum, drop it from the visited hash.
@@ -390,16 +389,22 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
       }
       if (LEARNED) {
         // Per-hop state: hop count, k-th and best distance, queue-head gap,
-        // distance evaluations; distances relative to the start distance.
+        // distance evaluations.  Distances enter through scale-free, bounded
+        // quantities: the progress span d0 - best, the top-k spread and the
+        // queue-head gap relative to that span (signed log), and the
+        // progress relative to |d0| + |best|.
         const int kk = min(p.k, tn);
         const float kth = key_float(T.at(C - tn + kk - 1, lane));
         const float best = key_float(T.at(C - tn, lane));
         const float head = nk != ~0ull ? key_float(nk) : kth;
+        const float span = fabsf(d0 - best) + 1e-6f * (fabsf(d0) + fabsf(best)) + 1e-30f;
+        const float r1 = (kth - best) / span;
+        const float r3 = (head - kth) / span;
         float f[MLP_IN];
         f[0] = __log2f(1.0f + static_cast<float>(hops)) * 0.1f;
-        f[1] = (kth - d0) * dscale;
-        f[2] = (best - d0) * dscale;
-        f[3] = (head - kth) * dscale;
+        f[1] = copysignf(log1pf(fabsf(r1)), r1);
+        f[2] = (d0 - best) / (fabsf(d0) + fabsf(best) + 1e-30f);
+        f[3] = copysignf(log1pf(fabsf(r3)), r3);
         f[4] = __log2f(1.0f + static_cast<float>(evals)) * 0.1f;
         if (trace && hops <= p.trace_hops && lane < TRACE_FIELDS) {
           float v = lane < MLP_IN ? f[0] : static_cast<float>(version);

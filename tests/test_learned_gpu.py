@@ -1,0 +1,62 @@
+"""Learned early exit (small workload: 15k x 16 cos, degree-16 graph, pq 200).
+
+Trained on traces of the plain search over training queries (seed 3) by the
+library's own kernels, evaluated on held-out queries (seed 2): the exit must
+cut the mean hop count substantially while keeping recall@10 within 0.01 of
+the plain search, and beat a fixed hop budget of the same mean hop count."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small(song):
+    from song_gb300 import datasets as D, groundtruth as GT
+    w = D.SMALL
+    data = D.base_vectors(w)
+    graph = song.graph_build(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150, batch_div=0)
+    train_q = D.query_vectors(w, nq=6000, seed=D.SEED_TRAIN)
+    test_q = D.query_vectors(w, nq=2000)
+    gt, _ = GT.exact_knn_fp64(data, test_q, 10, w.metric)
+    return w, data, graph, train_q, test_q, gt
+
+
+def test_trace_labels_are_monotone(song, small):
+    import torch
+    from song_gb300 import learned as LE
+    w, data, graph, train_q, _, _ = small
+    with song.Index(graph, data, w.shift, w.metric) as ix:
+        X, y = LE.trace_dataset(ix, train_q[:300], 200, 10)
+    X, y = X.cpu().numpy(), y.cpu().numpy()
+    # feature 0 is log2(1 + hop) / 10: consecutive within a query
+    hop = np.rint(2.0 ** (X[:, 0] * 10.0) - 1.0).astype(np.int64)
+    starts = np.nonzero(hop == 1)[0]
+    assert len(starts) == 300
+    for a, b in zip(starts, list(starts[1:]) + [len(hop)]):
+        assert np.array_equal(hop[a:b], np.arange(1, b - a + 1))
+        lab = y[a:b]
+        assert lab[-1] == 1.0 and np.all(np.diff(lab) >= 0)  # once final, always final
+
+
+def test_learned_exit_gains_over_plain_and_fixed_budget(song, small, capsys):
+    import torch
+    from song_gb300 import groundtruth as GT, learned as LE
+    w, data, graph, train_q, test_q, gt = small
+    pq, k = 200, 10
+    with song.Index(graph, data, w.shift, w.metric) as ix:
+        model = LE.fit(ix, train_q, pq, k, agreement=0.99, epochs=6)
+        dq = torch.from_numpy(test_q).cuda()
+        p_ids, p_hops, _ = LE.plain_stats(ix, dq, pq, k)
+        l_ids, l_hops, _ = LE.evaluate(ix, dq, pq, k, model.params, model.threshold, model.min_hops, model.every)
+        budget = int(round(l_hops.mean()))
+        f_ids, f_hops, _ = LE.evaluate(ix, dq, pq, k, max_hops=budget)
+    r_plain, r_learned, r_fixed = (GT.recall(x, gt, k) for x in (p_ids, l_ids, f_ids))
+    with capsys.disabled():
+        print("\n[learned exit] plain hops %.1f recall %.4f | learned hops %.1f recall %.4f | "
+              "fixed budget %d hops recall %.4f | threshold %.2f, %d samples"
+              % (p_hops.mean(), r_plain, l_hops.mean(), r_learned, budget, r_fixed, model.threshold,
+                 model.info["samples"]))
+    assert l_hops.mean() < 0.8 * p_hops.mean()
+    assert r_learned >= r_plain - 0.01
+    assert r_learned > r_fixed
