@@ -59,6 +59,12 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cache", default=os.environ.get("SONG_CACHE", "/tmp/song_gb300_cache"))
     p.add_argument("--curve", action="store_true", help="time every pq of the sweep (recall/throughput curve)")
+    p.add_argument("--mode", choices=["learned", "plain"], default="learned",
+                   help="headline path: learned early exit + BF16 (+FP32 rerank), or plain FP32")
+    p.add_argument("--rerank", type=int, default=100, help="FP32 re-ranked candidates (BF16 path)")
+    p.add_argument("--train-queries", type=int, default=20000)
+    p.add_argument("--recall-slack", type=float, default=0.004,
+                   help="validation recall@10 the exit may give up against the same search without it")
     return p.parse_args()
 
 
@@ -248,6 +254,64 @@ def run_reference(args, rank, world):
 # ours
 # ---------------------------------------------------------------------------
 
+class Runner:
+    """Device-buffer searches of one index over the resident query set."""
+
+    def __init__(self, ix, dq, k, stream):
+        import torch
+        self.ix, self.dq, self.k, self.stream = ix, dq, k, stream
+        nq = dq.shape[0]
+        self.out = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+        self.hops = torch.empty(nq, dtype=torch.int32, device="cuda")
+        self.evals = torch.empty(nq, dtype=torch.int32, device="cuda")
+
+    def __call__(self, pq, stats=False):
+        self.ix.search_device(self.dq.data_ptr(), self.dq.shape[0], pq, self.k, self.out.data_ptr(),
+                              self.hops.data_ptr() if stats else None, self.evals.data_ptr() if stats else None,
+                              self.stream.cuda_stream)
+
+    def ids(self):
+        import torch
+        torch.cuda.synchronize()
+        return self.out.cpu().numpy().view(np.uint64)
+
+
+def timed_steps(torch, run, pq, steps, flush, stream):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        run(pq)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def sweep_pq(torch, run, w, data, queries, gt_kth, k, target, curve, log_prefix):
+    """Smallest pq of PQ_SWEEP whose tie-aware recall@k reaches target."""
+    from song_gb300 import groundtruth as GT
+    nq = queries.shape[0]
+    out, chosen = [], 0
+    for cand in PQ_SWEEP:
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        run(cand)
+        t0.record(run.stream)
+        reps = 3 if curve else 1
+        for _ in range(reps):
+            run(cand)
+        t1.record(run.stream)
+        torch.cuda.synchronize()
+        qps = reps * nq / (t0.elapsed_time(t1) / 1000.0)
+        r = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
+        out.append([cand, round(r, 4), round(qps, 1)])
+        log("[bench] %s pq %d recall@10 %.4f  %.0f q/s" % (log_prefix, cand, r, qps))
+        if not chosen and r >= target:
+            chosen = cand
+            if not curve:
+                break
+    return (chosen or PQ_SWEEP[-1]), out
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -269,87 +333,80 @@ def main():
         if dist:
             dist.barrier()
 
+    import ctypes
+
     import song_gb300 as S
+    from song_gb300 import datasets as D
     from song_gb300 import groundtruth as GT
+    from song_gb300 import learned as LE
     S.load_library()
     w, data, queries, graph = load_workload(args, rank, barrier)
     nq, k = queries.shape[0], args.topk
     gt_ids, gt_kth = ground_truth(args, w, data, queries, k)
-
-    t = time.time()
-    ix = S.Index(graph, data, w.shift, w.metric, device=local)
-    log("[bench] index resident (%.2f GB) in %.1fs" % (ix.device_bytes() / 1e9, time.time() - t))
-
-    dq = torch.from_numpy(queries).cuda()
-    dout = torch.empty((nq, k), dtype=torch.int64, device="cuda")
-    dhops = torch.empty(nq, dtype=torch.int32, device="cuda")
-    devals = torch.empty(nq, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
-    sh = stream.cuda_stream
+    dq = torch.from_numpy(queries).cuda()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
-    def search(pq, stats=False):
-        ix.search_device(dq.data_ptr(), nq, pq, k, dout.data_ptr(),
-                         dhops.data_ptr() if stats else None, devals.data_ptr() if stats else None, sh)
+    # ---- plain FP32 search (the reference's semantics) ----------------------
+    t = time.time()
+    ix32 = S.Index(graph, data, w.shift, w.metric, device=local)
+    log("[bench] FP32 index resident (%.2f GB) in %.1fs" % (ix32.device_bytes() / 1e9, time.time() - t))
+    run32 = Runner(ix32, dq, k, stream)
+    pq32, sweep32 = (args.pq, []) if args.pq else sweep_pq(torch, run32, w, data, queries, gt_kth, k, args.recall,
+                                                            args.curve, "fp32")
+    run32(pq32, stats=True)
+    rec32 = GT.recall_tie_aware(run32.ids(), data, queries, gt_kth, w.metric, k)
+    ms32 = timed_steps(torch, run32, pq32, max(3, args.steps // 2), flush, stream)
+    plain = {"qps": round(nq / (statistics.median(ms32) / 1000.0), 1), "pq": pq32, "recall_at_10": round(rec32, 4),
+             "kernel_ms_median": round(statistics.median(ms32), 4),
+             "mean_hops": round(float(run32.hops.float().mean().item()), 2),
+             "mean_evals": round(float(run32.evals.float().mean().item()), 2), "pq_sweep_recall_qps": sweep32}
+    log("[bench] plain FP32: %s" % plain)
 
-    # pq sweep: smallest pq whose tie-aware recall@10 reaches the target
-    sweep = []
-    pq = args.pq
-    if pq == 0 or args.curve:
-        for cand in PQ_SWEEP:
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            search(cand)
-            t0.record(stream)
-            reps = 3 if args.curve else 1
-            for _ in range(reps):
-                search(cand)
-            t1.record(stream)
-            torch.cuda.synchronize()
-            qps = reps * nq / (t0.elapsed_time(t1) / 1000.0)
-            ids = dout.cpu().numpy().view(np.uint64)
-            r = GT.recall_tie_aware(ids, data, queries, gt_kth, w.metric, k)
-            sweep.append([cand, round(r, 4), round(qps, 1)])
-            log("[bench] pq %d recall@10 %.4f  %.0f q/s" % (cand, r, qps))
-            if pq == 0 and r >= args.recall:
-                pq = cand
-                if not args.curve:
-                    break
-        if pq == 0:
-            pq = PQ_SWEEP[-1]
-    search(pq, stats=True)
-    torch.cuda.synchronize()
-    ids = dout.cpu().numpy().view(np.uint64)
-    rec = GT.recall_tie_aware(ids, data, queries, gt_kth, w.metric, k)
+    # ---- learned early exit + BF16 storage + FP32 rerank (headline) ----------
+    mode = args.mode
+    if mode == "learned":
+        ix = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
+        ix.set_rerank(args.rerank)
+        run = Runner(ix, dq, k, stream)
+        train_q = D.query_vectors(w, nq=args.train_queries, seed=D.SEED_TRAIN)
+        pq, model, lrec = pq32, None, 0.0
+        tried = []
+        for cand in [c for c in PQ_SWEEP + [1023] if c >= pq32][:3]:
+            model = LE.fit(ix, train_q, cand, k, epochs=6, data=data, metric=w.metric,
+                           recall_slack=args.recall_slack, log=log)
+            ix.set_early_exit(model.params, model.threshold, model.min_hops, model.every)
+            run(cand, stats=True)
+            lrec = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
+            tried.append([cand, round(model.threshold, 2), round(lrec, 4)])
+            log("[bench] learned+bf16 pq %d threshold %.2f recall@10 %.4f" % (cand, model.threshold, lrec))
+            pq = cand
+            if lrec >= args.recall:
+                break
+        rec = lrec
+    else:
+        ix, run, pq, rec, model, tried = ix32, run32, pq32, rec32, None, []
+    run(pq, stats=True)
+    hops = run.hops.cpu().numpy().astype(np.int64)
+    evals = run.evals.cpu().numpy().astype(np.int64)
+    ids = run.ids()
     rec_ids = GT.recall(ids, gt_ids, k)
-    hops = dhops.cpu().numpy().astype(np.int64)
-    evals = devals.cpu().numpy().astype(np.int64)
-
-    # L2 flush buffer (larger than the 129 MB L2)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     sampler = ClockSampler(local)
     sampler.start()
-    # warm-up: at least W steps and at least ~1.5 s so the clock sampler sees load
     t0 = time.time()
     wsteps = 0
     while wsteps < args.warmup or time.time() - t0 < 1.5:
         flush.zero_()
-        search(pq)
+        run(pq)
         wsteps += 1
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     wall0 = time.perf_counter()
-    for i in range(args.steps):
-        flush.zero_()
-        ev[i][0].record(stream)
-        search(pq)
-        ev[i][1].record(stream)
-    torch.cuda.synchronize()
+    kernel_ms = timed_steps(torch, run, pq, args.steps, flush, stream)
     wall = time.perf_counter() - wall0
     barrier()
-    kernel_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(kernel_ms) / 1000.0
     if dist:
         tt = torch.tensor([total_s], dtype=torch.float64, device="cuda")
@@ -362,7 +419,6 @@ def main():
     pinned.numpy()[:] = queries
     hq = pinned.numpy()
     out_host = torch.empty((nq, k), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
-    import ctypes
     L = S.load_library()
     for _ in range(max(1, args.warmup)):
         S._check(L.song_search(ix._h, hq.ctypes.data_as(ctypes.c_void_p), nq, pq, k,
@@ -385,8 +441,14 @@ def main():
     e2e = world * nq * args.steps / e2e_s
 
     # roofline: algorithmic bytes per launch / mean kernel time
-    row_bytes = 4 * (((w.dim + 3) // 4) * 4)
-    alg_bytes = int((4 * w.dim * nq) + hops.sum() * (1 << w.shift) * 4 + evals.sum() * row_bytes + nq * k * 8)
+    if mode == "learned":
+        row_bytes = 2 * (((w.dim + 7) // 8) * 8)
+        rerank_rows = min(args.rerank if args.rerank > 0 else pq, pq)
+    else:
+        row_bytes = 4 * (((w.dim + 3) // 4) * 4)
+        rerank_rows = 0
+    alg_bytes = int((4 * w.dim * nq) + hops.sum() * (1 << w.shift) * 4 + evals.sum() * row_bytes
+                    + nq * rerank_rows * 4 * w.dim + nq * k * 8)
     mean_s = (sum(kernel_ms) / len(kernel_ms)) / 1000.0
     achieved = alg_bytes / mean_s / 1e9
     peaks = {}
@@ -396,12 +458,12 @@ def main():
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic_scale.json")
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         try:
-            tj = json.load(open(tp))
-            if tj.get("pq") == pq and tj.get("workload") == w.name:
-                traffic = tj.get("dram_bytes_per_launch")
+            tj = json.load(open(tp)).get("%s/%s/pq%d" % (w.name, mode, pq))
+            if tj:
+                traffic = int(tj["dram_bytes_per_query"] * nq)
         except Exception:
             traffic = None
 
@@ -421,19 +483,28 @@ def main():
             cpu = {"value": None, "error": repr(e)}
 
     if rank == 0:
+        desc = ("learned early exit + BF16 storage + FP32 rerank" if mode == "learned" else "plain FP32 search")
         line = {
-            "metric": "queries/s at recall@10>=%.2f, %s (plain FP32 search)" % (args.recall, w.name),
+            "metric": "queries/s at recall@10>=%.2f, %s (%s)" % (args.recall, w.name, desc),
             "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": wsteps, "ms_per_step": round(1000 * total_s / args.steps, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 storage, f32 accumulate, f32 rerank" if mode == "learned" else "f32",
             "data": "synthetic (seeded Gaussian mixture, SIFT1M shape)",
             "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric,
                        "graph": "shift %d (FIXED_DEGREE %d, SEARCH_DEGREE %d), batch-parallel build div %d"
                                 % (w.shift, w.fixed_degree, w.search_degree, args.build_div),
-                       "pq": pq, "top_k": k, "queries_per_step": nq, "recall_at_10": round(rec, 4),
-                       "recall_at_10_ids": round(rec_ids, 4), "pq_sweep_recall_qps": sweep,
+                       "mode": mode, "pq": pq, "top_k": k, "queries_per_step": nq,
+                       "recall_at_10": round(rec, 4), "recall_at_10_ids": round(rec_ids, 4),
                        "mean_hops": round(float(hops.mean()), 2), "mean_evals": round(float(evals.mean()), 2),
-                       "l2": "flushed between steps (256 MB write); index 512 MB > L2",
+                       "plain_fp32": plain,
+                       "speedup_vs_plain_fp32": round(value / plain["qps"], 3),
+                       "learned": None if model is None else {
+                           "threshold": model.threshold, "min_hops": model.min_hops, "rerank": args.rerank,
+                           "train_queries": args.train_queries, "recall_slack": args.recall_slack,
+                           "tried_pq_threshold_recall": tried,
+                           "train": {kk: model.info[kk] for kk in ("samples", "positive", "trace_s", "train_s", "losses", "chosen")}},
+                       "l2": "flushed between steps (256 MB write); index > L2",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -449,7 +520,9 @@ def main():
             "wall_s_timed": round(wall, 4),
         }
         print(json.dumps(line), flush=True)
-    ix.free()
+    if ix is not ix32:
+        ix.free()
+    ix32.free()
     if dist:
         dist.destroy_process_group()
 

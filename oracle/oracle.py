@@ -21,7 +21,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 
 L2, IP, COS = 0, 1, 2
 METRICS = {"l2": L2, "ip": IP, "cos": COS}
-MODE_REF, MODE_LEX = 0, 1
+MODE_REF, MODE_LEX, MODE_LEX_EXACT = 0, 1, 2
 NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 EV_NAMES = {1: "POP", 2: "FINISH", 3: "TEVICT", 4: "SKIP", 5: "INSERT", 6: "QEVICT", 7: "TEST",

@@ -338,6 +338,9 @@ static void lk_insert(lk_t *a, int *n, lk_t e) {
 typedef struct {
   int pq;
   int maxdeg;
+  uint16_t *cnt;      /* LEX_EXACT: visited multiplicity per vertex */
+  uint64_t *touched;  /* LEX_EXACT: vertices with cnt != 0 to clear */
+  size_t ntouched, tcap;
   kp_t *q, *t;   /* REF */
   lk_t *lq, *lt; /* LEX */
   int32_t *tab;
@@ -346,8 +349,9 @@ typedef struct {
   uint64_t *tmp_out;
 } kscratch;
 
-static int kscratch_init(kscratch *s, int pq, int maxdeg) {
+static int kscratch_init(kscratch *s, int pq, int maxdeg, uint64_t n) {
   memset(s, 0, sizeof *s);
+  s->cnt = (uint16_t *)calloc((size_t)n, sizeof(uint16_t));
   s->pq = pq;
   s->maxdeg = maxdeg;
   s->q = (kp_t *)malloc(sizeof(kp_t) * (size_t)(pq + 3));
@@ -358,10 +362,12 @@ static int kscratch_init(kscratch *s, int pq, int maxdeg) {
   s->cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(maxdeg + 1));
   s->cdist = (float *)malloc(sizeof(float) * (size_t)(maxdeg + 1));
   s->tmp_out = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)pq);
-  return s->q && s->t && s->lq && s->lt && s->tab && s->cand && s->cdist && s->tmp_out ? 0 : -1;
+  return s->cnt && s->q && s->t && s->lq && s->lt && s->tab && s->cand && s->cdist && s->tmp_out ? 0 : -1;
 }
 
 static void kscratch_free(kscratch *s) {
+  free(s->cnt);
+  free(s->touched);
   free(s->q);
   free(s->t);
   free(s->lq);
@@ -395,6 +401,40 @@ static inline const float *row(const orc_index *ix, uint64_t id) {
   return ix->data + id * (uint64_t)ix->dim;
 }
 
+/* Visited-set operations: FixHash (modes REF and LEX) or an exact multiset
+ * (mode LEX_EXACT). */
+typedef struct {
+  int exact;
+  int32_t *tab;
+  int cap;
+  kscratch *s;
+} vset;
+
+static void vs_add(vset *v, uint64_t id) {
+  if (!v->exact) {
+    orc_fixhash_add(v->tab, v->cap, (int32_t)id);
+    return;
+  }
+  kscratch *s = v->s;
+  if (s->cnt[id]++ == 0) {
+    if (s->ntouched == s->tcap) {
+      s->tcap = s->tcap ? 2 * s->tcap : 1024;
+      s->touched = (uint64_t *)realloc(s->touched, sizeof(uint64_t) * s->tcap);
+    }
+    s->touched[s->ntouched++] = id;
+  }
+}
+static void vs_del(vset *v, uint64_t id) {
+  if (!v->exact) {
+    orc_fixhash_del(v->tab, v->cap, (int32_t)id);
+    return;
+  }
+  if (v->s->cnt[id]) v->s->cnt[id]--;
+}
+static int vs_test(const vset *v, uint64_t id) {
+  return v->exact ? v->s->cnt[id] != 0 : orc_fixhash_test(v->tab, v->cap, (int32_t)id);
+}
+
 /* warp_astar_accelerator.h:111-335 for one query (mode REF), or the GB300
  * kernel's specification of it (mode LEX).  Returns the number of vertices in
  * the top-pq list at the end. */
@@ -404,7 +444,13 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
   const int cap = 8 * pq; /* FixHash<int, TOPK*4*2>, warp_astar_accelerator.h:59-61 */
   const int shift = ix->shift;
   int32_t *tab = s->tab;
-  orc_fixhash_init(tab, cap);
+  vset vs = {mode == ORC_MODE_LEX_EXACT, tab, cap, s};
+  if (vs.exact) {
+    for (size_t i = 0; i < s->ntouched; ++i) s->cnt[s->touched[i]] = 0;
+    s->ntouched = 0;
+  } else {
+    orc_fixhash_init(tab, cap);
+  }
 
   int hs = 1, ts = 0; /* REF: SMMH size (+1 dummy slot) and heap size */
   int qn = 0;         /* LEX: queue length (ts shared) */
@@ -419,7 +465,7 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
     lk_t e = {d0, 0, 0};
     lk_insert(s->lq, &qn, e);
   }
-  orc_fixhash_add(tab, cap, 0);
+  vs_add(&vs, 0);
 
   for (;;) {
     uint64_t now_id;
@@ -438,7 +484,7 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
       now_d = now.d;
     }
     ev(L, ORC_EV_POP, now_id, now_d);
-    orc_fixhash_del(tab, cap, (int32_t)now_id);
+    vs_del(&vs, now_id);
     /* :191 finish test uses <= */
     float tmax = mode == ORC_MODE_REF ? (ts > 0 ? (float)s->t[0].d : 0.0f)
                                       : (ts > 0 ? s->lt[ts - 1].d : 0.0f);
@@ -452,10 +498,10 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
       kp_t e = {(double)now_d, now_id};
       s->t[ts++] = e;
       bh_push(s->t, ts);
-      orc_fixhash_add(tab, cap, (int32_t)now_id);
+      vs_add(&vs, now_id);
       if (ts > pq) {
         kp_t top = s->t[0];
-        orc_fixhash_del(tab, cap, (int32_t)top.id);
+        vs_del(&vs, top.id);
         bh_pop(s->t, ts);
         --ts;
         ev(L, ORC_EV_TEVICT, top.id, (float)top.d);
@@ -463,10 +509,10 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
     } else {
       lk_t e = {now_d, 0, now_id};
       lk_insert(s->lt, &ts, e);
-      orc_fixhash_add(tab, cap, (int32_t)now_id);
+      vs_add(&vs, now_id);
       if (ts > pq) {
         lk_t top = s->lt[ts - 1];
-        orc_fixhash_del(tab, cap, (int32_t)top.id);
+        vs_del(&vs, top.id);
         --ts;
         ev(L, ORC_EV_TEVICT, top.id, top.d);
       }
@@ -477,7 +523,7 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
     int m = 0;
     for (int i = 1; i <= degree; ++i) {
       uint64_t nb = grow[i];
-      if (orc_fixhash_test(tab, cap, (int32_t)nb)) continue;
+      if (vs_test(&vs, nb)) continue;
       s->cand[m++] = nb;
     }
     /* :237-287 distances */
@@ -497,11 +543,11 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
         }
         kp_t e = {(double)d, id};
         smmh_insert(s->q, &hs, e);
-        orc_fixhash_add(tab, cap, (int32_t)id);
+        vs_add(&vs, id);
         ev(L, ORC_EV_INSERT, id, d);
         if (hs >= pq + 2) {
           kp_t mx = s->q[2];
-          orc_fixhash_del(tab, cap, (int32_t)mx.id);
+          vs_del(&vs, mx.id);
           smmh_pop_max(s->q, &hs);
           ev(L, ORC_EV_QEVICT, mx.id, (float)mx.d);
         }
@@ -512,11 +558,11 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
         }
         lk_t e = {d, 0, id};
         lk_insert(s->lq, &qn, e);
-        orc_fixhash_add(tab, cap, (int32_t)id);
+        vs_add(&vs, id);
         ev(L, ORC_EV_INSERT, id, d);
         if (qn >= pq + 1) {
           lk_t mx = s->lq[qn - 1];
-          orc_fixhash_del(tab, cap, (int32_t)mx.id);
+          vs_del(&vs, mx.id);
           --qn;
           ev(L, ORC_EV_QEVICT, mx.id, mx.d);
         }
@@ -572,7 +618,7 @@ static int maxdeg_of(const orc_index *ix) { return (1 << ix->shift) - 1; }
 static void *kworker(void *arg) {
   job_t *j = (job_t *)arg;
   kscratch s;
-  if (kscratch_init(&s, j->pq, maxdeg_of(j->ix)) != 0) {
+  if (kscratch_init(&s, j->pq, maxdeg_of(j->ix), j->ix->n) != 0) {
     j->err = 1;
     kscratch_free(&s);
     return NULL;
@@ -616,7 +662,7 @@ int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq,
                       int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                       int32_t *popped, int nthreads) {
   if (check_index(ix) || !queries || !out || nq < 0 || pq < 2 || pq > 4095) return -1;
-  if (mode != ORC_MODE_REF && mode != ORC_MODE_LEX) return -1;
+  if (mode != ORC_MODE_REF && mode != ORC_MODE_LEX && mode != ORC_MODE_LEX_EXACT) return -1;
   job_t j;
   memset(&j, 0, sizeof j);
   j.ix = ix;
@@ -636,7 +682,7 @@ int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int m
                           uint64_t *out, orc_event *log, int cap, int *n_events) {
   if (check_index(ix) || !query || !out || pq < 2 || pq > 4095) return -1;
   kscratch s;
-  if (kscratch_init(&s, pq, maxdeg_of(ix)) != 0) {
+  if (kscratch_init(&s, pq, maxdeg_of(ix), ix->n) != 0) {
     kscratch_free(&s);
     return -1;
   }

@@ -43,7 +43,9 @@ extern "C" {
 #endif
 
 enum { ORC_L2 = 0, ORC_IP = 1, ORC_COS = 2 };      /* KernelFixedDegreeGraph<0|1|2> */
-enum { ORC_MODE_REF = 0, ORC_MODE_LEX = 1 };
+/* ORC_MODE_LEX_EXACT: LEX with an exact visited multiset instead of FixHash
+ * (the learned/low-precision kernel's visited set, which never loses an entry). */
+enum { ORC_MODE_REF = 0, ORC_MODE_LEX = 1, ORC_MODE_LEX_EXACT = 2 };
 
 /* Output slot that the search did not fill (fewer than pq vertices popped). */
 #define ORC_NO_ID UINT64_MAX

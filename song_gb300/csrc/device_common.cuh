@@ -212,6 +212,98 @@ struct VisitedHash {
 };
 
 // ---------------------------------------------------------------------------
+// Exact visited set for the learned / low-precision path, which makes no
+// bit-parity claim with the reference: power-of-two capacity (>= 4*pq), a
+// multiplicative slot function, linear probing and the textbook
+// backward-shift delete (an entry moves into the hole when its home slot is
+// not cyclically inside (hole, position]), so no entry is ever lost.  Half the
+// shared memory of VisitedHash at the same pq, and a two-instruction slot.
+// ---------------------------------------------------------------------------
+struct ExactVisited {
+  int32_t *tab;
+  int cap;       // power of two
+  int log2cap;
+
+  __device__ __forceinline__ int slot(uint32_t id) const {
+    return static_cast<int>((id * 0x9E3779B1u) >> (32 - log2cap));  // cap >= 32
+  }
+  __device__ __forceinline__ int wrap(int s) const { return s & (cap - 1); }
+
+  __device__ __forceinline__ void clear(int lane) {
+    for (int i = lane; i < cap; i += 32) tab[i] = FH_EMPTY;
+    __syncwarp();
+  }
+
+  __device__ __forceinline__ bool test(uint32_t id) const {
+    int c = slot(id);
+    for (int i = 0; i < cap; ++i) {
+      const int32_t v = tab[c];
+      if (v == FH_EMPTY) return false;
+      if (v == static_cast<int32_t>(id)) return true;
+      c = (c + 1) & (cap - 1);
+    }
+    return false;
+  }
+
+  __device__ __forceinline__ void add(uint32_t id, int lane) {
+    int base = slot(id);
+    for (int w = 0; w * 32 < cap + 32; ++w) {
+      const int s = wrap(base + lane);
+      const int32_t v = tab[s];
+      const unsigned b = __ballot_sync(FULL, v == FH_EMPTY);
+      if (b) {
+        if (lane == __ffs(b) - 1) tab[s] = static_cast<int32_t>(id);
+        break;
+      }
+      base = wrap(base + 32);
+    }
+    __syncwarp();
+  }
+
+  __device__ __forceinline__ void del(uint32_t id, int lane) {
+    const int32_t x = static_cast<int32_t>(id);
+    int base = slot(id), h = -1;
+    for (int w = 0; w * 32 < cap + 32; ++w) {
+      const int s = wrap(base + lane);
+      const int32_t v = tab[s];
+      const unsigned be = __ballot_sync(FULL, v == FH_EMPTY);
+      const unsigned bm = __ballot_sync(FULL, v == x);
+      const unsigned before = be ? ((1u << (__ffs(be) - 1)) - 1u) : FULL;
+      const unsigned hit = bm & before;
+      if (hit) {
+        h = wrap(base + __ffs(hit) - 1);
+        break;
+      }
+      if (be) return;
+      base = wrap(base + 32);
+    }
+    if (h < 0) return;
+    int nbase = wrap(h + 1);
+    for (int w = 0; w * 32 < cap + 32; ++w) {
+      const int s = wrap(nbase + lane);
+      const int32_t v = tab[s];
+      const int home = v >= 0 ? slot(static_cast<uint32_t>(v)) : 0;
+      const unsigned be = __ballot_sync(FULL, v == FH_EMPTY);
+      const int run = be ? __ffs(be) - 1 : 32;
+      for (int i = 0; i < run; ++i) {
+        const int j = wrap(nbase + i);
+        const int hm = __shfl_sync(FULL, home, i);
+        const int32_t val = __shfl_sync(FULL, v, i);
+        if (((j - hm) & (cap - 1)) >= ((j - h) & (cap - 1))) {
+          if (lane == 0) tab[h] = val;
+          h = j;
+        }
+      }
+      __syncwarp();
+      if (be) break;
+      nbase = wrap(nbase + 32);
+    }
+    if (lane == 0) tab[h] = FH_EMPTY;
+    __syncwarp();
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Sorted queue in a power-of-two ring of uint64 keys: a[(head + i) & mask],
 // i in [0, n), ascending.  Used for the candidate queue (pops at the head)
 // and for the top-pq list (head fixed at 0).

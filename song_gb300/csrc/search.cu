@@ -39,11 +39,19 @@ struct Layout {
   int cap, H, S;
 };
 
-Layout make_layout(const DeviceIndex &ix, int pq) {
+// FixHash capacity 8*pq (the reference's TOPK*4*2) for the plain kernel; the
+// learned kernel's exact set: the power of two >= max(32, 4*pq).
+int exact_cap(int pq) {
+  int c = 32;
+  while (c < 4 * pq) c <<= 1;
+  return c;
+}
+
+Layout make_layout(const DeviceIndex &ix, int pq, bool learned) {
   Layout L;
   L.H = stage_rows(ix.row_bytes);
   L.S = queue_segment(pq);
-  L.cap = 8 * pq;
+  L.cap = learned ? exact_cap(pq) : 8 * pq;
   uint32_t off = 2u * L.H * ix.row_bytes;
   off = align_up(off, 16);
   L.off_mbar = off;
@@ -108,11 +116,12 @@ int get_shape(const void *fn, uint32_t warp_bytes, uint32_t extra, int *wpb, int
   return 0;
 }
 
-uint32_t search_warp_bytes(const DeviceIndex &ix, int pq) { return make_layout(ix, pq).warp_bytes; }
+uint32_t search_warp_bytes(const DeviceIndex &ix, int pq) { return make_layout(ix, pq, false).warp_bytes; }
 
 int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t stream) {
   if (c.nq <= 0) return 0;
-  const Layout L = make_layout(ix, c.pq);
+  const bool learned = c.mlp != nullptr || c.trace != nullptr || c.exit_max_hops > 0;
+  const Layout L = make_layout(ix, c.pq, learned);
   Params p;
   p.rows = static_cast<const uint8_t *>(ix.rows);
   p.row_bytes = ix.row_bytes;
@@ -139,6 +148,8 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
   p.off_hash = L.off_hash;
   p.cap = L.cap;
   p.magic = ~0ull / static_cast<uint64_t>(L.cap);
+  p.log2cap = 0;
+  while ((1 << p.log2cap) < L.cap) ++p.log2cap;
   p.mlp = c.mlp;
   p.exit_threshold = c.exit_threshold;
   p.exit_min_hops = c.exit_min_hops;
@@ -147,7 +158,6 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
   p.trace = c.trace;
   p.trace_hops = c.trace_hops;
   p.trace_final = c.trace_final;
-  const bool learned = c.mlp != nullptr || c.trace != nullptr || c.exit_max_hops > 0;
   if (learned) {
     if (ix.storage == 2) return -1;
     return launch_learned(p, ix.storage, ix.metric, L.H, L.S, stream);

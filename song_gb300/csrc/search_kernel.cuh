@@ -72,7 +72,8 @@ struct Params {
   uint32_t warp_bytes;
   uint32_t off_mbar, off_cand, off_q, off_hash;
   int cap;
-  uint64_t magic;
+  uint64_t magic;  // VisitedHash (plain kernel)
+  int log2cap;     // ExactVisited (learned kernel)
   // learned variant
   const __nv_bfloat16 *mlp;  // MLP_NPARAM weights (BF16), null = no early exit
   float exit_threshold;
@@ -252,6 +253,19 @@ __device__ __forceinline__ float mlp_logit(const __nv_bfloat16 *w, const float f
   return __fadd_rn(z, __bfloat162float(w[MLP_B3]));
 }
 
+// The plain kernel keeps the reference's FixHash (bit parity); the learned
+// kernel, which makes no parity claim, uses the smaller exact set.
+template <bool LEARNED>
+struct VisitedOf {
+  using type = VisitedHash;
+  __device__ static VisitedHash make(int32_t *tab, const Params &p) { return VisitedHash{tab, p.cap, p.magic}; }
+};
+template <>
+struct VisitedOf<true> {
+  using type = ExactVisited;
+  __device__ static ExactVisited make(int32_t *tab, const Params &p) { return ExactVisited{tab, p.cap, p.log2cap}; }
+};
+
 template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
 __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(const Params p) {
   extern __shared__ __align__(128) uint8_t smem_raw[];
@@ -263,7 +277,8 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
   uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + p.off_mbar);
   uint32_t *cbuf = reinterpret_cast<uint32_t *>(ws + p.off_cand);
   float *qv = reinterpret_cast<float *>(ws + p.off_q);
-  VisitedHash vh{reinterpret_cast<int32_t *>(ws + p.off_hash), p.cap, p.magic};
+  typename VisitedOf<LEARNED>::type vh =
+      VisitedOf<LEARNED>::make(reinterpret_cast<int32_t *>(ws + p.off_hash), p);
   RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
   constexpr int C = RegQueue<S>::C;
 
@@ -327,7 +342,7 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
       // :191 finish test (<=) against the list maximum.
       if (tn == p.pq && key_dist(T.max()) <= key_dist(now)) break;
       ++hops;
-      if (LEARNED) {  // does `now` enter the current top-k?
+      if (LEARNED && trace) {  // does `now` enter the current top-k?
         if (tn < p.k || now < T.at(C - tn + p.k - 1, lane)) ++version;
       }
       // :198-210 move it to the top-pq list (when full, `now` is below the
@@ -388,6 +403,8 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
         }
       }
       if (LEARNED) {
+        const bool check = p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= p.k;
+        if (trace || check) {
         // Per-hop state: hop count, k-th and best distance, queue-head gap,
         // distance evaluations.  Distances enter through scale-free, bounded
         // quantities: the progress span d0 - best, the top-k spread and the
@@ -412,9 +429,7 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
           for (int i = 1; i < MLP_IN; ++i) v = lane == i ? f[i] : v;
           trace[static_cast<size_t>(hops - 1) * TRACE_FIELDS + lane] = v;
         }
-        if (p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= p.k) {
-          const float z = mlp_logit(wmlp, f, lane);
-          if (z >= p.exit_threshold) break;  // converged: stop before the pq budget
+        if (check && mlp_logit(wmlp, f, lane) >= p.exit_threshold) break;  // converged
         }
         if (p.exit_max_hops > 0 && hops >= p.exit_max_hops) break;
       }

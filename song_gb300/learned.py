@@ -116,13 +116,22 @@ def evaluate(index: Index, dq, pq: int, k: int, params=None, threshold=0.0, min_
         index.set_hop_limit(0)
 
 
+THRESHOLDS = [round(4.0 - 0.25 * i, 2) for i in range(23)]  # 4.0 .. -1.5
+
+
 def fit(index: Index, train_queries: np.ndarray, pq: int, k: int, val_frac: float = 0.2,
-        agreement: float = 0.995, min_hops: int = 8, every: int = 1, epochs: int = 6,
-        max_samples_per_query: int = 256, seed: int = 0, log=None) -> ExitModel:
-    """Trace, train, and choose the most permissive threshold whose stopped
-    queries keep the plain top-k on at least `agreement` of the validation
-    queries."""
+        agreement: float = 0.995, min_hops: int = 8, every: int = 4, epochs: int = 6,
+        max_samples_per_query: int = 256, seed: int = 0, data=None, metric=None,
+        recall_slack: float = None, log=None) -> ExitModel:
+    """Trace, train, and choose the threshold on held-out training queries.
+
+    With `data`/`metric` and `recall_slack`, the chosen threshold is the most
+    permissive one whose validation recall@k (tie-aware, against an FP64
+    exact kNN) stays within `recall_slack` of the search without exit;
+    otherwise the most permissive one that keeps the exit-free top-k on at
+    least `agreement` of the validation queries."""
     import torch
+    from . import groundtruth as GT
     nval = max(1, int(len(train_queries) * val_frac))
     tq, vq = train_queries[nval:], train_queries[:nval]
     t0 = time.time()
@@ -130,20 +139,33 @@ def fit(index: Index, train_queries: np.ndarray, pq: int, k: int, val_frac: floa
     t_trace = time.time() - t0
     params, losses, t_train = train(X, y, epochs=epochs, seed=seed)
     dv = torch.from_numpy(np.ascontiguousarray(vq, np.float32)).cuda()
-    base_ids, base_hops, _ = plain_stats(index, dv, pq, k)
-    best = None
-    curve = []
-    for thr in (6.0, 5.0, 4.0, 3.0, 2.5, 2.0, 1.5, 1.0, 0.5, 0.0, -0.5, -1.0):
+    # the exit-free search of the same kernel: a hop budget no query reaches
+    base_ids, base_hops, _ = evaluate(index, dv, pq, k, max_hops=1 << 30)
+    use_recall = data is not None and recall_slack is not None
+    if use_recall:
+        _, kth = GT.exact_knn_fp64(data, vq, k, metric)
+        base_rec = GT.recall_tie_aware(base_ids, data, vq, kth, metric, k)
+    best, curve = None, []
+    for thr in THRESHOLDS:
         ids, hops, _ = evaluate(index, dv, pq, k, params, thr, min_hops, every)
         agree = float((np.sort(ids, axis=1) == np.sort(base_ids, axis=1)).all(axis=1).mean())
-        curve.append((thr, agree, float(hops.mean())))
-        if agree >= agreement:
-            best = (thr, agree, float(hops.mean()))
+        row = [thr, round(agree, 4), round(float(hops.mean()), 2)]
+        ok = agree >= agreement
+        if use_recall:
+            rec = GT.recall_tie_aware(ids, data, vq, kth, metric, k)
+            row.append(round(rec, 4))
+            ok = rec >= base_rec - recall_slack
+        curve.append(row)
+        if ok:
+            best = row
+        elif best is not None:
+            break  # thresholds only get more permissive from here
     if best is None:
-        best = (curve[0][0], curve[0][1], curve[0][2])
+        best = curve[0]
     info = dict(samples=int(X.shape[0]), positive=float(y.mean().item()), trace_s=round(t_trace, 2),
                 train_s=round(t_train, 2), losses=[round(float(v), 4) for v in losses],
-                val_plain_hops=float(base_hops.mean()), threshold_curve=curve, chosen=best)
+                val_plain_hops=float(base_hops.mean()), threshold_curve=curve, chosen=best,
+                val_recall_no_exit=round(base_rec, 4) if use_recall else None)
     if log:
         log("[learned] %s" % info)
     return ExitModel(params=params, threshold=best[0], min_hops=min_hops, every=every, pq=pq, k=k, info=info)

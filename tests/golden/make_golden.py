@@ -89,6 +89,49 @@ def make_fixhash_case():
     np.savez_compressed(os.path.join(HERE, "fixhash_ops.npz"), **out)
 
 
+def make_fma_probe():
+    """Query / vector pairs whose L2 order differs between fused (nvcc's
+    default contraction) and separate multiply-add in the kernel's
+    lane-strided sums (only possible for dim > 32, where a lane adds more
+    than one term), each embedded in a 128-vertex graph searched at pq 100.
+    Expected ids come from the harness (reference containers, FMA); the ids
+    the oracle gives without FMA are stored too and must differ."""
+    rng = np.random.default_rng(7)
+    dim, n, shift, pq = 128, 128, 5, 100
+    probes = []
+    while len(probes) < 4:
+        q = rng.standard_normal(dim).astype(np.float32)
+        a = (q + rng.standard_normal(dim).astype(np.float32)).astype(np.float32)
+        b = a.copy()
+        for i in rng.choice(dim, 3, replace=False):
+            b[i] = np.nextafter(b[i], np.float32(np.inf) if rng.random() < .5 else np.float32(-np.inf))
+        fa, fb = O.kernel_distance(O.L2, q, a, True), O.kernel_distance(O.L2, q, b, True)
+        na, nb = O.kernel_distance(O.L2, q, a, False), O.kernel_distance(O.L2, q, b, False)
+        if (fa < fb) != (na < nb) and fa != fb and na != nb:
+            probes.append((q, a, b))
+    graph = np.zeros((n, 1 << shift), np.uint64)
+    for v in range(n):
+        graph[v, 0] = 31
+        graph[v, 1:32] = [(v + 1 + j) % n for j in range(31)]
+    graph = graph.reshape(-1)
+    datas, queries, fma_ids, nofma_ids = [], [], [], []
+    for q, a, b in probes:
+        far = (q + 8.0 * rng.standard_normal((n, dim))).astype(np.float32)
+        far[1], far[2] = a, b
+        ids, _, _, popped = O.ref_kernel_search(far, graph, shift, O.L2, q[None, :], pq)
+        assert popped[0] == pq
+        ox = O.OracleIndex(far, graph, shift, O.L2)
+        nf, *_ = ox.kernel_search(q[None, :], pq, O.MODE_REF, use_fma=False)
+        assert not np.array_equal(nf, ids)
+        datas.append(far)
+        queries.append(q)
+        fma_ids.append(ids[0])
+        nofma_ids.append(nf[0])
+    np.savez_compressed(os.path.join(HERE, "fma_probe.npz"), data=np.array(datas), queries=np.array(queries),
+                        graph=graph.astype(np.uint32), shift=np.int32(shift), pq=np.int32(pq),
+                        fma_ids=np.array(fma_ids), nofma_ids=np.array(nofma_ids))
+
+
 def main():
     if not O.ref_available(4) or not O.ref_available(5):
         raise SystemExit("oracle/_ref not built: run bash oracle/build_ref.sh first")
@@ -97,6 +140,8 @@ def main():
         print("wrote search_%s.npz" % case[0])
     make_fixhash_case()
     print("wrote fixhash_ops.npz")
+    make_fma_probe()
+    print("wrote fma_probe.npz")
 
 
 if __name__ == "__main__":

@@ -45,7 +45,7 @@ def test_learned_exit_gains_over_plain_and_fixed_budget(song, small, capsys):
     w, data, graph, train_q, test_q, gt = small
     pq, k = 200, 10
     with song.Index(graph, data, w.shift, w.metric) as ix:
-        model = LE.fit(ix, train_q, pq, k, agreement=0.99, epochs=6)
+        model = LE.fit(ix, train_q, pq, k, epochs=6, data=data, metric=w.metric, recall_slack=0.005)
         dq = torch.from_numpy(test_q).cuda()
         p_ids, p_hops, _ = LE.plain_stats(ix, dq, pq, k)
         l_ids, l_hops, _ = LE.evaluate(ix, dq, pq, k, model.params, model.threshold, model.min_hops, model.every)
@@ -57,6 +57,29 @@ def test_learned_exit_gains_over_plain_and_fixed_budget(song, small, capsys):
               "fixed budget %d hops recall %.4f | threshold %.2f, %d samples"
               % (p_hops.mean(), r_plain, l_hops.mean(), r_learned, budget, r_fixed, model.threshold,
                  model.info["samples"]))
-    assert l_hops.mean() < 0.8 * p_hops.mean()
+    assert l_hops.mean() < 0.85 * p_hops.mean()
     assert r_learned >= r_plain - 0.01
     assert r_learned > r_fixed
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_learned_kernel_without_exit_matches_exact_visited_oracle(song, oracle, storage):
+    """The learned kernel keeps an exact visited set (no parity claim with the
+    reference's FixHash); with the exit disabled it must equal the oracle's
+    LEX_EXACT search over the stored rows bit for bit."""
+    import torch
+    from conftest import load_golden
+    from song_gb300 import learned as LE
+    for name in ("l2_s5_d32", "cos_s4_d16"):
+        g = load_golden(name)
+        shift, metric = int(g["shift"]), int(g["metric"])
+        with song.Index(g["graph"], g["data"], shift, metric, storage=storage) as ix:
+            ix.set_rerank(0)
+            deq = song.dequantize_rows(ix.rows(), storage, g["data"].shape[1])
+            ox = oracle.OracleIndex(deq, g["graph"], shift, metric)
+            dq = torch.from_numpy(g["queries"]).cuda()
+            for pq in (10, 100):
+                ids, hops, evals = LE.evaluate(ix, dq, pq, pq, max_hops=1 << 30)
+                o_ids, o_hops, o_evals, _ = ox.kernel_search(g["queries"], pq, oracle.MODE_LEX_EXACT)
+                assert np.array_equal(ids, o_ids), (name, storage, pq)
+                assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)

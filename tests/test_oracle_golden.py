@@ -96,3 +96,17 @@ def test_cpu_distance_matches_double_accumulation(oracle):
         d = np.float32(a - b)
         ref += float(np.float32(d * d))
     assert oracle.cpu_distance(oracle.L2, x, q) == ref
+
+
+def test_fma_probe_separates_contraction(oracle):
+    """dim 128 L2 cases whose order depends on fused vs separate multiply-add:
+    the oracle with FMA reproduces the reference containers' ids, without FMA
+    it does not."""
+    z = np.load(GOLDEN + "/fma_probe.npz")
+    graph = z["graph"].astype(np.uint64)
+    for i in range(z["data"].shape[0]):
+        ox = oracle.OracleIndex(z["data"][i], graph, int(z["shift"]), oracle.L2)
+        f, *_ = ox.kernel_search(z["queries"][i:i + 1], int(z["pq"]), oracle.MODE_REF, use_fma=True)
+        nf, *_ = ox.kernel_search(z["queries"][i:i + 1], int(z["pq"]), oracle.MODE_REF, use_fma=False)
+        assert np.array_equal(f[0], z["fma_ids"][i]) and np.array_equal(nf[0], z["nofma_ids"][i])
+        assert not np.array_equal(f[0], nf[0])
