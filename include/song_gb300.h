@@ -180,6 +180,27 @@ int song_search_trace_device(song_index *index, const float *d_queries, int nq, 
                              int trace_hops, float *d_trace, int32_t *d_final, uint64_t *d_out,
                              int32_t *d_hops, int32_t *d_evals, void *stream);
 
+/* Continuous-batching server over one resident index (no counterpart in the
+ * reference).  A persistent kernel on `sm_fraction` of the GPU's warp slots
+ * searches queries as soon as they are published; requests of 1..slot_queries
+ * queries with their own pq (<= max_pq) and k (<= max_k) are admitted while
+ * one of `slots` query/result slots is free and otherwise wait, in order, for
+ * one (admission by memory).  Queries and ids stay in mapped pinned host
+ * memory.  A request's ids are exactly what song_search returns for it alone.
+ * F32 storage.  One host thread at a time per server. */
+typedef struct song_server song_server;
+int song_server_create(song_index *index, int max_pq, int max_k, int slots, int slot_queries,
+                       float sm_fraction, song_server **out);
+/* Copies the queries and queues the request; *ticket identifies it. */
+int song_server_submit(song_server *server, const float *queries, int nq, int pq, int k,
+                       uint64_t *ticket);
+/* Up to `max` tickets of requests completed since the last poll. */
+int song_server_poll(song_server *server, uint64_t *tickets, int max, int *n_done);
+/* The nq x k ids of a completed request; frees its slot for waiting requests. */
+int song_server_result(song_server *server, uint64_t ticket, uint64_t *out, int *nq, int *k);
+/* Drains published work, stops the kernel and frees the server. */
+int song_server_destroy(song_server *server);
+
 /* Size of the fixed device scratch array used by song_search_noalloc. */
 #define SONG_NOALLOC_SCRATCH_BYTES (16u << 20)
 

@@ -34,6 +34,7 @@ EXPORTED = [
     "song_astar_search_batch", "song_graph_build", "song_debug_fixhash", "song_search_noalloc",
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
     "song_index_set_hop_limit", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
+    "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
 ]
 MLP_PARAMS = 1281
 TRACE_FIELDS = 6
@@ -100,6 +101,16 @@ def load_library():
     L.song_mlp_grad.argtypes = [P, P, P, i32, P, P, P]
     L.song_mlp_forward.restype = i32
     L.song_mlp_forward.argtypes = [P, i32, P, P]
+    L.song_server_create.restype = i32
+    L.song_server_create.argtypes = [P, i32, i32, i32, i32, ctypes.c_float, ctypes.POINTER(P)]
+    L.song_server_submit.restype = i32
+    L.song_server_submit.argtypes = [P, P, i32, i32, i32, ctypes.POINTER(ctypes.c_uint64)]
+    L.song_server_poll.restype = i32
+    L.song_server_poll.argtypes = [P, P, i32, ctypes.POINTER(i32)]
+    L.song_server_result.restype = i32
+    L.song_server_result.argtypes = [P, ctypes.c_uint64, P, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.song_server_destroy.restype = i32
+    L.song_server_destroy.argtypes = [P]
     L.song_search_noalloc.restype = i32
     L.song_search_noalloc.argtypes = [P, P, i32, i32, i32, P]
     L.song_debug_fixhash.restype = i32

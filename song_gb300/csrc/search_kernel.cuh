@@ -254,17 +254,216 @@ __device__ __forceinline__ float mlp_logit(const __nv_bfloat16 *w, const float f
 }
 
 // The plain kernel keeps the reference's FixHash (bit parity); the learned
-// kernel, which makes no parity claim, uses the smaller exact set.
+// kernel, which makes no parity claim, uses the smaller exact set.  Both are
+// sized per query from its pq.
 template <bool LEARNED>
 struct VisitedOf {
   using type = VisitedHash;
-  __device__ static VisitedHash make(int32_t *tab, const Params &p) { return VisitedHash{tab, p.cap, p.magic}; }
+  __device__ static VisitedHash make(int32_t *tab, int pq) {
+    const int cap = 8 * pq;
+    return VisitedHash{tab, cap, ~0ull / static_cast<uint64_t>(cap)};
+  }
 };
 template <>
 struct VisitedOf<true> {
   using type = ExactVisited;
-  __device__ static ExactVisited make(int32_t *tab, const Params &p) { return ExactVisited{tab, p.cap, p.log2cap}; }
+  __device__ static ExactVisited make(int32_t *tab, int pq) {
+    int lg = 5;
+    while ((1 << lg) < 4 * pq) ++lg;
+    return ExactVisited{tab, 1 << lg, lg};
+  }
 };
+
+// The warp's shared-memory slice and barrier phases.
+struct WarpCtx {
+  uint8_t *stage;
+  uint64_t *mbar;
+  uint32_t *cbuf;
+  float *qv;
+  int32_t *tab;
+  const __nv_bfloat16 *wmlp;
+  uint32_t ph0, ph1;
+};
+
+struct QueryStats {
+  int hops, evals, version;
+};
+
+// One query: the search of warp_astar_accelerator.h:111-335 with the query
+// vector at qsrc, queue bound pq, k ids written ascending to o.  `trace`
+// (LEARNED) receives the per-hop features or is null.  False if a bulk copy
+// never completed.
+template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
+__device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const float *qsrc, int pq, int k,
+                                          uint64_t *o, float *trace, QueryStats &st, int lane) {
+  typename VisitedOf<LEARNED>::type vh = VisitedOf<LEARNED>::make(w.tab, pq);
+  RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
+  constexpr int C = RegQueue<S>::C;
+  const int nslots = 1 << p.shift;
+  for (int j = lane; j < p.dim; j += 32) w.qv[j] = qsrc[j];
+  vh.clear(lane);
+  // Adjacency row of vertex 0, the first vertex popped.
+  uint32_t next_id = 0;
+  uint32_t a_next = lane < nslots ? __ldg(p.adj + lane) : 0u;
+
+  // warp_astar_accelerator.h:115-176: distance to vertex 0, queue = {0}.
+  float cd;
+  if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, 1, 0u, cd, lane)) {
+    return false;
+  }
+  const float d0 = __shfl_sync(FULL, cd, 0);
+  int qn = 0, tn = 0;
+  Q.clear();
+  T.clear();
+  Q.insert_grow(make_key(d0, 0u), lane);
+  qn = 1;
+  vh.add(0u, lane);
+  int hops = 0, evals = 1;
+  int version = 0;  // number of changes of the top-k set (LEARNED)
+
+  while (qn > 0) {
+    // :186-193 pop the minimum, drop it from the visited hash.
+    uint64_t qh;  // queue minimum after the pop
+    const uint64_t now = Q.pop_min(qn, lane, &qh);
+    --qn;
+    const uint32_t now_id = key_id(now);
+    uint32_t a = a_next;
+    if (now_id != next_id)  // not taken: the prefetch predicts the pop exactly
+      a = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(now_id) << p.shift) + lane) : 0u;
+    vh.del(now_id, lane);
+    // :191 finish test (<=) against the list maximum.
+    if (tn == pq && key_dist(T.max()) <= key_dist(now)) break;
+    ++hops;
+    if (LEARNED && trace) {  // does `now` enter the current top-k?
+      if (tn < k || now < T.at(C - tn + k - 1, lane)) ++version;
+    }
+    // :198-210 move it to the top-pq list (when full, `now` is below the
+    // list maximum, which is the one dropped).
+    if (tn < pq) {
+      T.insert_grow(now, lane);
+      ++tn;
+      vh.add(now_id, lane);
+    } else {
+      const uint64_t ev = T.max();
+      T.insert_evict(now, lane);
+      vh.add(now_id, lane);
+      vh.del(key_id(ev), lane);
+    }
+    // :211-224 neighbours not in the visited hash, in row order.
+    const int deg = static_cast<int>(__shfl_sync(FULL, a, 0));
+    const bool isnb = lane >= 1 && lane <= deg;
+    const bool fresh = isnb && !vh.test(a);
+    const unsigned fm = __ballot_sync(FULL, fresh);
+    const int m = __popc(fm);
+    if (fresh) w.cbuf[__popc(fm & lanemask_lt())] = a;
+    __syncwarp();
+    const uint32_t cid = lane < m ? w.cbuf[lane] : 0u;
+    // :237-287 distances.
+    if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, m, cid, cd, lane))
+      return false;
+    evals += m;
+    // The next vertex popped is the smaller of the queue head and the best
+    // candidate (the select-insert rule can only reject candidates above a
+    // full queue's maximum); start loading its adjacency row now so that it
+    // arrives while the candidates are inserted.
+    const uint64_t ck = lane < m ? make_key(cd, cid) : ~0ull;
+    const uint64_t cmin = warp_min_u64(ck);
+    const uint64_t nk = cmin < qh ? cmin : qh;
+    if (nk != ~0ull) {
+      next_id = key_id(nk);
+      a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
+    }
+    // :297-322 select-insert in candidate order.
+    for (int c = 0; c < m; ++c) {
+      const float d = __shfl_sync(FULL, cd, c);
+      const uint32_t id = __shfl_sync(FULL, cid, c);
+      const uint64_t key = make_key(d, id);
+      if (qn < pq) {
+        Q.insert_grow(key, lane);
+        ++qn;
+        vh.add(id, lane);
+      } else {
+        const uint64_t qmax = Q.max();
+        if (key_dist(qmax) < key_dist(key)) continue;
+        // inserted, then the larger of the two leaves (:315-320)
+        const uint64_t ev = key < qmax ? qmax : key;
+        Q.insert_evict(key, lane);
+        vh.add(id, lane);
+        vh.del(key_id(ev), lane);
+      }
+    }
+    if (LEARNED) {
+      const bool check = p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= k;
+      if (trace || check) {
+      // Per-hop state: hop count, k-th and best distance, queue-head gap,
+      // distance evaluations.  Distances enter through scale-free, bounded
+      // quantities: the progress span d0 - best, the top-k spread and the
+      // queue-head gap relative to that span (signed log), and the
+      // progress relative to |d0| + |best|.
+      const int kk = min(k, tn);
+      const float kth = key_float(T.at(C - tn + kk - 1, lane));
+      const float best = key_float(T.at(C - tn, lane));
+      const float head = nk != ~0ull ? key_float(nk) : kth;
+      const float span = fabsf(d0 - best) + 1e-6f * (fabsf(d0) + fabsf(best)) + 1e-30f;
+      const float r1 = (kth - best) / span;
+      const float r3 = (head - kth) / span;
+      float f[MLP_IN];
+      f[0] = __log2f(1.0f + static_cast<float>(hops)) * 0.1f;
+      f[1] = copysignf(log1pf(fabsf(r1)), r1);
+      f[2] = (d0 - best) / (fabsf(d0) + fabsf(best) + 1e-30f);
+      f[3] = copysignf(log1pf(fabsf(r3)), r3);
+      f[4] = __log2f(1.0f + static_cast<float>(evals)) * 0.1f;
+      if (trace && hops <= p.trace_hops && lane < TRACE_FIELDS) {
+        float v = lane < MLP_IN ? f[0] : static_cast<float>(version);
+#pragma unroll
+        for (int i = 1; i < MLP_IN; ++i) v = lane == i ? f[i] : v;
+        trace[static_cast<size_t>(hops - 1) * TRACE_FIELDS + lane] = v;
+      }
+      if (check && mlp_logit(w.wmlp, f, lane) >= p.exit_threshold) break;  // converged
+      }
+      if (p.exit_max_hops > 0 && hops >= p.exit_max_hops) break;
+    }
+  }
+
+  if (STORAGE != 0 && p.rerank > 0) {
+    // FP32 re-rank of the best `rerank` entries of the list, then the first k.
+    const int R = min(max(p.rerank, k), tn);
+    int rn = 0;
+    Q.clear();
+    for (int base = 0; base < R; base += 4) {
+      uint32_t ids[4];
+      const int cnt = min(4, R - base);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) ids[i] = i < cnt ? key_id(T.at(C - tn + base + i, lane)) : 0u;
+      float d[4];
+      fp32_distances4<METRIC>(p, w.qv, ids, cnt, d, lane);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (i < cnt) {
+          Q.insert_grow(make_key(d[i], ids[i]), lane);
+          ++rn;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      const int r = Q.rank_of(j, rn, lane);
+      if (r >= 0 && r < k) o[r] = static_cast<uint64_t>(key_id(Q.v[j]));
+    }
+    for (int i = rn + lane; i < k; i += 32) o[i] = ~0ull;
+  } else {
+    // :331-335 ascending ids; slots past the list length get UINT64_MAX.
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      const int r = T.rank_of(j, tn, lane);
+      if (r >= 0 && r < k) o[r] = static_cast<uint64_t>(key_id(T.v[j]));
+    }
+    for (int i = tn + lane; i < k; i += 32) o[i] = ~0ull;
+  }
+  st.hops = hops;
+  st.evals = evals;
+  st.version = version;
+  return true;
+}
 
 template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
 __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(const Params p) {
@@ -273,209 +472,48 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
   const int wib = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   uint8_t *ws = smem_raw + static_cast<size_t>(wib) * p.warp_bytes;
-  uint8_t *stage = ws;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(ws + p.off_mbar);
-  uint32_t *cbuf = reinterpret_cast<uint32_t *>(ws + p.off_cand);
-  float *qv = reinterpret_cast<float *>(ws + p.off_q);
-  typename VisitedOf<LEARNED>::type vh =
-      VisitedOf<LEARNED>::make(reinterpret_cast<int32_t *>(ws + p.off_hash), p);
-  RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
-  constexpr int C = RegQueue<S>::C;
-
+  WarpCtx w;
+  w.stage = ws;
+  w.mbar = reinterpret_cast<uint64_t *>(ws + p.off_mbar);
+  w.cbuf = reinterpret_cast<uint32_t *>(ws + p.off_cand);
+  w.qv = reinterpret_cast<float *>(ws + p.off_q);
+  w.tab = reinterpret_cast<int32_t *>(ws + p.off_hash);
   __nv_bfloat16 *wmlp = reinterpret_cast<__nv_bfloat16 *>(smem_raw + static_cast<size_t>(nwarps) * p.warp_bytes);
+  w.wmlp = wmlp;
   if (LEARNED) {
     if (p.mlp)
       for (int i = threadIdx.x; i < MLP_NPARAM; i += blockDim.x) wmlp[i] = p.mlp[i];
     __syncthreads();
   }
-
   if (lane == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    mbar_init(&w.mbar[0], 1);
+    mbar_init(&w.mbar[1], 1);
     fence_mbar_init();
   }
   __syncwarp();
-  uint32_t ph0 = 0, ph1 = 0;
-  const int nslots = 1 << p.shift;
+  w.ph0 = 0;
+  w.ph1 = 0;
 
   for (;;) {
     uint32_t qid = 0;
     if (lane == 0) qid = atomicAdd(p.counter, 1u);
     qid = __shfl_sync(FULL, qid, 0);
     if (qid >= static_cast<uint32_t>(p.nq)) break;
-
-    const float *qsrc = p.queries + static_cast<size_t>(qid) * p.dim;
-    for (int j = lane; j < p.dim; j += 32) qv[j] = qsrc[j];
-    vh.clear(lane);
-    // Adjacency row of vertex 0, the first vertex popped.
-    uint32_t next_id = 0;
-    uint32_t a_next = lane < nslots ? __ldg(p.adj + lane) : 0u;
-
-    // warp_astar_accelerator.h:115-176: distance to vertex 0, queue = {0}.
-    float cd;
-    if (!gather_distances<METRIC, STORAGE, H>(p, stage, mbar, ph0, ph1, qv, 1, 0u, cd, lane)) {
+    float *trace = nullptr;
+    if (LEARNED && p.trace) trace = p.trace + static_cast<size_t>(qid) * p.trace_hops * TRACE_FIELDS;
+    QueryStats st;
+    if (!run_query<METRIC, STORAGE, H, S, LEARNED>(p, w, p.queries + static_cast<size_t>(qid) * p.dim, p.pq,
+                                                   p.k, p.out + static_cast<size_t>(qid) * p.k, trace, st,
+                                                   lane)) {
       if (lane == 0) atomicOr(p.error, 1);
       return;
     }
-    const float d0 = __shfl_sync(FULL, cd, 0);
-    int qn = 0, tn = 0;
-    Q.clear();
-    T.clear();
-    Q.insert_grow(make_key(d0, 0u), lane);
-    qn = 1;
-    vh.add(0u, lane);
-    int hops = 0, evals = 1;
-    int version = 0;  // number of changes of the top-k set (LEARNED)
-    float *trace = nullptr;
-    if (LEARNED && p.trace) trace = p.trace + static_cast<size_t>(qid) * p.trace_hops * TRACE_FIELDS;
-
-    while (qn > 0) {
-      // :186-193 pop the minimum, drop it from the visited hash.
-      uint64_t qh;  // queue minimum after the pop
-      const uint64_t now = Q.pop_min(qn, lane, &qh);
-      --qn;
-      const uint32_t now_id = key_id(now);
-      uint32_t a = a_next;
-      if (now_id != next_id)  // not taken: the prefetch predicts the pop exactly
-        a = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(now_id) << p.shift) + lane) : 0u;
-      vh.del(now_id, lane);
-      // :191 finish test (<=) against the list maximum.
-      if (tn == p.pq && key_dist(T.max()) <= key_dist(now)) break;
-      ++hops;
-      if (LEARNED && trace) {  // does `now` enter the current top-k?
-        if (tn < p.k || now < T.at(C - tn + p.k - 1, lane)) ++version;
-      }
-      // :198-210 move it to the top-pq list (when full, `now` is below the
-      // list maximum, which is the one dropped).
-      if (tn < p.pq) {
-        T.insert_grow(now, lane);
-        ++tn;
-        vh.add(now_id, lane);
-      } else {
-        const uint64_t ev = T.max();
-        T.insert_evict(now, lane);
-        vh.add(now_id, lane);
-        vh.del(key_id(ev), lane);
-      }
-      // :211-224 neighbours not in the visited hash, in row order.
-      const int deg = static_cast<int>(__shfl_sync(FULL, a, 0));
-      const bool isnb = lane >= 1 && lane <= deg;
-      const bool fresh = isnb && !vh.test(a);
-      const unsigned fm = __ballot_sync(FULL, fresh);
-      const int m = __popc(fm);
-      if (fresh) cbuf[__popc(fm & lanemask_lt())] = a;
-      __syncwarp();
-      const uint32_t cid = lane < m ? cbuf[lane] : 0u;
-      // :237-287 distances.
-      if (!gather_distances<METRIC, STORAGE, H>(p, stage, mbar, ph0, ph1, qv, m, cid, cd, lane)) {
-        if (lane == 0) atomicOr(p.error, 1);
-        return;
-      }
-      evals += m;
-      // The next vertex popped is the smaller of the queue head and the best
-      // candidate (the select-insert rule can only reject candidates above a
-      // full queue's maximum); start loading its adjacency row now so that it
-      // arrives while the candidates are inserted.
-      const uint64_t ck = lane < m ? make_key(cd, cid) : ~0ull;
-      const uint64_t cmin = warp_min_u64(ck);
-      const uint64_t nk = cmin < qh ? cmin : qh;
-      if (nk != ~0ull) {
-        next_id = key_id(nk);
-        a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
-      }
-      // :297-322 select-insert in candidate order.
-      for (int c = 0; c < m; ++c) {
-        const float d = __shfl_sync(FULL, cd, c);
-        const uint32_t id = __shfl_sync(FULL, cid, c);
-        const uint64_t key = make_key(d, id);
-        if (qn < p.pq) {
-          Q.insert_grow(key, lane);
-          ++qn;
-          vh.add(id, lane);
-        } else {
-          const uint64_t qmax = Q.max();
-          if (key_dist(qmax) < key_dist(key)) continue;
-          // inserted, then the larger of the two leaves (:315-320)
-          const uint64_t ev = key < qmax ? qmax : key;
-          Q.insert_evict(key, lane);
-          vh.add(id, lane);
-          vh.del(key_id(ev), lane);
-        }
-      }
-      if (LEARNED) {
-        const bool check = p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= p.k;
-        if (trace || check) {
-        // Per-hop state: hop count, k-th and best distance, queue-head gap,
-        // distance evaluations.  Distances enter through scale-free, bounded
-        // quantities: the progress span d0 - best, the top-k spread and the
-        // queue-head gap relative to that span (signed log), and the
-        // progress relative to |d0| + |best|.
-        const int kk = min(p.k, tn);
-        const float kth = key_float(T.at(C - tn + kk - 1, lane));
-        const float best = key_float(T.at(C - tn, lane));
-        const float head = nk != ~0ull ? key_float(nk) : kth;
-        const float span = fabsf(d0 - best) + 1e-6f * (fabsf(d0) + fabsf(best)) + 1e-30f;
-        const float r1 = (kth - best) / span;
-        const float r3 = (head - kth) / span;
-        float f[MLP_IN];
-        f[0] = __log2f(1.0f + static_cast<float>(hops)) * 0.1f;
-        f[1] = copysignf(log1pf(fabsf(r1)), r1);
-        f[2] = (d0 - best) / (fabsf(d0) + fabsf(best) + 1e-30f);
-        f[3] = copysignf(log1pf(fabsf(r3)), r3);
-        f[4] = __log2f(1.0f + static_cast<float>(evals)) * 0.1f;
-        if (trace && hops <= p.trace_hops && lane < TRACE_FIELDS) {
-          float v = lane < MLP_IN ? f[0] : static_cast<float>(version);
-#pragma unroll
-          for (int i = 1; i < MLP_IN; ++i) v = lane == i ? f[i] : v;
-          trace[static_cast<size_t>(hops - 1) * TRACE_FIELDS + lane] = v;
-        }
-        if (check && mlp_logit(wmlp, f, lane) >= p.exit_threshold) break;  // converged
-        }
-        if (p.exit_max_hops > 0 && hops >= p.exit_max_hops) break;
-      }
-    }
-
-    uint64_t *o = p.out + static_cast<size_t>(qid) * p.k;
-    if (STORAGE != 0 && p.rerank > 0) {
-      // FP32 re-rank of the best `rerank` entries of the list, then the first k.
-      const int R = min(max(p.rerank, p.k), tn);
-      int rn = 0;
-      Q.clear();
-      for (int base = 0; base < R; base += 4) {
-        uint32_t ids[4];
-        const int cnt = min(4, R - base);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) ids[i] = i < cnt ? key_id(T.at(C - tn + base + i, lane)) : 0u;
-        float d[4];
-        fp32_distances4<METRIC>(p, qv, ids, cnt, d, lane);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (i < cnt) {
-            Q.insert_grow(make_key(d[i], ids[i]), lane);
-            ++rn;
-          }
-      }
-#pragma unroll
-      for (int j = 0; j < S; ++j) {
-        const int r = Q.rank_of(j, rn, lane);
-        if (r >= 0 && r < p.k) o[r] = static_cast<uint64_t>(key_id(Q.v[j]));
-      }
-      for (int i = rn + lane; i < p.k; i += 32) o[i] = ~0ull;
-    } else {
-      // :331-335 ascending ids; slots past the list length get UINT64_MAX.
-#pragma unroll
-      for (int j = 0; j < S; ++j) {
-        const int r = T.rank_of(j, tn, lane);
-        if (r >= 0 && r < p.k) o[r] = static_cast<uint64_t>(key_id(T.v[j]));
-      }
-      for (int i = tn + lane; i < p.k; i += 32) o[i] = ~0ull;
-    }
     if (lane == 0) {
-      if (p.hops) p.hops[qid] = hops;
-      if (p.evals) p.evals[qid] = evals;
+      if (p.hops) p.hops[qid] = st.hops;
+      if (p.evals) p.evals[qid] = st.evals;
       if (LEARNED && p.trace_final) {
-        p.trace_final[2 * qid] = version;
-        p.trace_final[2 * qid + 1] = min(hops, p.trace_hops);
+        p.trace_final[2 * qid] = st.version;
+        p.trace_final[2 * qid + 1] = min(st.hops, p.trace_hops);
       }
     }
     __syncwarp();
