@@ -137,7 +137,8 @@ int song_index_rows(const song_index *index, uint64_t first, uint64_t count, voi
  * 5 -> 32 -> 32 -> 1 (ReLU) reads, after every `every`-th hop from hop
  * `min_hops` on, the query's state (log hop count; the top-k spread and the
  * queue-head gap relative to the progress span d0 - best, as signed logs;
- * the progress (d0 - best) / (|d0| + |best|); log distance evaluations) and
+ * log of the hops since the top-k set last changed; log distance
+ * evaluations) and
  * stops the search when its logit >= threshold; queries it
  * never trusts run the plain search to its finish rule.  weights: the
  * SONG_MLP_PARAMS FP32 parameters (W1[32][5], b1[32], W2[32][32], b2[32],

@@ -22,6 +22,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 L2, IP, COS = 0, 1, 2
 METRICS = {"l2": L2, "ip": IP, "cos": COS}
 MODE_REF, MODE_LEX, MODE_LEX_EXACT = 0, 1, 2
+TRACE_FIELDS = 6  # 5 early-exit features + number of changes of the top-k set
 NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 EV_NAMES = {1: "POP", 2: "FINISH", 3: "TEVICT", 4: "SKIP", 5: "INSERT", 6: "QEVICT", 7: "TEST",
@@ -80,6 +81,8 @@ def lib():
         L.orc_kernel_search_log.argtypes = [P, P, i32, i32, i32, P, P, i32, P]
         L.orc_classify.restype = i32
         L.orc_classify.argtypes = [P, i32, P, i32, P]
+        L.orc_kernel_search_trace.restype = i32
+        L.orc_kernel_search_trace.argtypes = [P, P, i32, i32, i32, i32, i32, P, P, P, P, P, P]
         L.orc_cpu_search.restype = i32
         L.orc_cpu_search.argtypes = [P, P, i32, i32, P, P, i32]
         L.orc_fixhash_hash.restype = i32
@@ -145,6 +148,21 @@ class OracleIndex:
         if n.value > cap:
             raise ValueError("event log overflow")
         return out, log[:n.value]
+
+    def kernel_search_trace(self, query, pq, k, trace_hops, mode=MODE_LEX_EXACT, use_fma=True):
+        """One query with the learned kernel's per-hop trace
+        (song_oracle.h: orc_kernel_search_trace).  Returns (trace
+        [traced x 6], final top-k version, ids, hops, evals)."""
+        q = np.ascontiguousarray(query, dtype=np.float32).reshape(-1)
+        tr = np.zeros((trace_hops, TRACE_FIELDS), dtype=np.float32)
+        fin, traced, hops, evals = (ctypes.c_int32(0) for _ in range(4))
+        out = np.empty(pq, dtype=np.uint64)
+        rc = lib().orc_kernel_search_trace(self.ref, _ptr(q), pq, k, mode, int(use_fma), trace_hops, _ptr(tr),
+                                           ctypes.byref(fin), ctypes.byref(traced), _ptr(out),
+                                           ctypes.byref(hops), ctypes.byref(evals))
+        if rc != 0:
+            raise ValueError("orc_kernel_search_trace failed")
+        return tr[:traced.value], fin.value, out, hops.value, evals.value
 
     def cpu_search(self, queries, k, nthreads=None):
         q = np.ascontiguousarray(queries, dtype=np.float32)

@@ -438,9 +438,39 @@ static int vs_test(const vset *v, uint64_t id) {
 /* warp_astar_accelerator.h:111-335 for one query (mode REF), or the GB300
  * kernel's specification of it (mode LEX).  Returns the number of vertices in
  * the top-pq list at the end. */
+/* Per-hop early-exit features (LEX modes), as the learned search kernel
+ * computes them after each hop's select-insert: log2(1 + hops) / 10; the
+ * top-k spread (kth - best) and the queue-head gap (head - kth) relative to
+ * the progress span |d0 - best| as signed log1p; log2(1 + hops since the
+ * top-k set last changed) / 10; log2(1 + distance evaluations) / 10; then the
+ * number of changes of the top-k set so far. */
+typedef struct {
+  int k, trace_hops;
+  float *trace; /* trace_hops x ORC_TRACE_FIELDS */
+  int32_t version, traced;
+} ktrace;
+
+static void trace_hop(ktrace *tr, const kscratch *s, int qn, int ts, float d0, int hops, int evals,
+                      int last_change) {
+  if (!tr || hops > tr->trace_hops) return;
+  const float kth = ts >= tr->k ? s->lt[tr->k - 1].d : s->lt[ts - 1].d;
+  const float best = s->lt[0].d;
+  const float head = qn > 0 ? s->lq[0].d : kth;
+  const float span = fabsf(d0 - best) + 1e-6f * (fabsf(d0) + fabsf(best)) + 1e-30f;
+  const float r1 = (kth - best) / span;
+  const float r3 = (head - kth) / span;
+  float *f = tr->trace + (size_t)(hops - 1) * ORC_TRACE_FIELDS;
+  f[0] = log2f(1.0f + (float)hops) * 0.1f;
+  f[1] = copysignf(log1pf(fabsf(r1)), r1);
+  f[2] = log2f(1.0f + (float)(hops - last_change)) * 0.1f;
+  f[3] = copysignf(log1pf(fabsf(r3)), r3);
+  f[4] = log2f(1.0f + (float)evals) * 0.1f;
+  f[5] = (float)tr->version;
+}
+
 static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, int use_fma,
                        kscratch *s, uint64_t *out, int32_t *hops_out, int32_t *evals_out,
-                       evlog *L) {
+                       evlog *L, ktrace *tr) {
   const int cap = 8 * pq; /* FixHash<int, TOPK*4*2>, warp_astar_accelerator.h:59-61 */
   const int shift = ix->shift;
   int32_t *tab = s->tab;
@@ -455,6 +485,7 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
   int hs = 1, ts = 0; /* REF: SMMH size (+1 dummy slot) and heap size */
   int qn = 0;         /* LEX: queue length (ts shared) */
   int hops = 0, evals = 0;
+  int last_change = 0;
 
   float d0 = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, 0), use_fma);
   evals = 1;
@@ -508,6 +539,10 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
       }
     } else {
       lk_t e = {now_d, 0, now_id};
+      if (tr && (ts < tr->k || lk_less(e, s->lt[tr->k - 1]))) { /* enters the top-k */
+        ++tr->version;
+        last_change = hops;
+      }
       lk_insert(s->lt, &ts, e);
       vs_add(&vs, now_id);
       if (ts > pq) {
@@ -568,7 +603,9 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
         }
       }
     }
+    if (mode != ORC_MODE_REF) trace_hop(tr, s, qn, ts, d0, hops, evals, last_change);
   }
+  if (tr) tr->traced = hops < tr->trace_hops ? hops : tr->trace_hops;
 
   /* :331-335 output, ascending.  With fewer than pq popped vertices the
    * reference reads before its heap array (undefined); both modes put the
@@ -628,7 +665,7 @@ static void *kworker(void *arg) {
     if (i >= j->nq) break;
     int32_t h = 0, e = 0;
     int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim, j->pq, j->mode,
-                         j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL);
+                         j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL, NULL);
     if (j->hops) j->hops[i] = h;
     if (j->evals) j->evals[i] = e;
     if (j->popped) j->popped[i] = ts;
@@ -687,8 +724,27 @@ int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int m
     return -1;
   }
   evlog L = {log, cap, 0};
-  ksearch_one(ix, query, pq, mode, use_fma, &s, out, NULL, NULL, &L);
+  ksearch_one(ix, query, pq, mode, use_fma, &s, out, NULL, NULL, &L, NULL);
   if (n_events) *n_events = L.n;
+  kscratch_free(&s);
+  return 0;
+}
+
+int orc_kernel_search_trace(const orc_index *ix, const float *query, int pq, int k, int mode,
+                            int use_fma, int trace_hops, float *trace, int32_t *final_version,
+                            int32_t *traced, uint64_t *out, int32_t *hops, int32_t *evals) {
+  if (check_index(ix) || !query || !out || !trace || pq < 2 || pq > 4095 || k < 1 || k > pq ||
+      trace_hops < 1 || mode == ORC_MODE_REF)
+    return -1;
+  kscratch s;
+  if (kscratch_init(&s, pq, maxdeg_of(ix), ix->n) != 0) {
+    kscratch_free(&s);
+    return -1;
+  }
+  ktrace tr = {k, trace_hops, trace, 0, 0};
+  ksearch_one(ix, query, pq, mode, use_fma, &s, out, hops, evals, NULL, &tr);
+  if (final_version) *final_version = tr.version;
+  if (traced) *traced = tr.traced;
   kscratch_free(&s);
   return 0;
 }

@@ -102,6 +102,16 @@ int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq,
 int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int mode, int use_fma,
                           uint64_t *out, orc_event *log, int cap, int *n_events);
 
+/* One LEX / LEX_EXACT query with the learned search kernel's per-hop trace:
+ * for hop h < min(hops, trace_hops), trace[h*ORC_TRACE_FIELDS + 0..4] are the
+ * early-exit features after hop h+1 and [.. + 5] the number of changes of the
+ * top-k set so far; *final_version gets that number at the end and *traced
+ * min(hops, trace_hops).  out: pq ids.  Returns 0, or -1 on bad arguments. */
+#define ORC_TRACE_FIELDS 6
+int orc_kernel_search_trace(const orc_index *ix, const float *query, int pq, int k, int mode,
+                            int use_fma, int trace_hops, float *trace, int32_t *final_version,
+                            int32_t *traced, uint64_t *out, int32_t *hops, int32_t *evals);
+
 /* Compare the REF and LEX logs of one query.  Returns 0 if identical, 1 if the
  * first difference is a tie (same event kind, same distance, different id),
  * 2 if it is anything else.  *at gets the index of the first difference. */

@@ -13,7 +13,7 @@
 //     right; neither needs the insertion position, only per-slot compares
 //     against the new key and one shuffle for the lane boundary;
 //   * removing the minimum (position C-n) is the only operation that touches
-//     a dynamic position: one select pass over the S slots.
+//     a run-time position: a select tree reads it, one select pass clears it.
 // All operations are warp-uniform.
 #pragma once
 
@@ -36,15 +36,12 @@ struct RegQueue {
   // Largest live key (0 when empty).
   __device__ __forceinline__ uint64_t max() const { return __shfl_sync(FULL, v[S - 1], 31); }
 
-  // Key at position pos (broadcast).
-  // (Selections compare the full position, lane*S + j, rather than a slot
-  // index: written as "slot == r" the compiler turns the loop into a dynamic
-  // array index and moves the array to local memory.)
+  // Key at the warp-uniform position pos (broadcast).  (Selections never
+  // index v[] with a run-time value: the compiler would move the array to
+  // local memory.)
   __device__ __forceinline__ uint64_t at(int pos, int lane) const {
-    uint64_t x = 0;
-#pragma unroll
-    for (int j = 0; j < S; ++j) x = (lane * S + j) == pos ? v[j] : x;
-    return __shfl_sync(FULL, x, pos / S);
+    const int owner = pos / S;
+    return __shfl_sync(FULL, slot(pos - owner * S), owner);
   }
 
   // Insert, n -> n + 1 (requires n < C): keys below `key` move one place left.
@@ -71,20 +68,38 @@ struct RegQueue {
     }
   }
 
+  // v[r] for a warp-uniform slot r in [0, S): a binary tree of selects on
+  // the bits of r (S - 1 selects, depth log2 S; a chain of S compares would
+  // serialise S dependent selects).
+  __device__ __forceinline__ uint64_t slot(int r) const {
+    uint64_t t[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) t[j] = v[j];
+#pragma unroll
+    for (int w = 1; w < S; w <<= 1) {
+      const bool b = (r & w) != 0;
+#pragma unroll
+      for (int j = 0; j + w < S; j += 2 * w) t[j] = b ? t[j + w] : t[j];
+    }
+    return t[0];
+  }
+
   // Remove the minimum of n >= 1 live keys; returns it, and the new minimum
   // in *next (~0 if none is left).
   __device__ __forceinline__ uint64_t pop_min(int n, int lane, uint64_t *next) {
-    const int pos = C - n;
-    uint64_t x = 0, y = ~0ull;
-#pragma unroll
-    for (int j = 0; j < S; ++j) {
-      const int q = lane * S + j;
-      x = q == pos ? v[j] : x;
-      y = q == pos + 1 ? v[j] : y;
-      v[j] = q == pos ? 0ull : v[j];
+    const int pos = C - n;  // warp-uniform
+    const int owner = pos / S, r = pos - owner * S;
+    const uint64_t m = __shfl_sync(FULL, slot(r), owner);
+    if (n > 1) {
+      const int pos1 = pos + 1;
+      const int owner1 = pos1 / S;
+      *next = __shfl_sync(FULL, slot(pos1 - owner1 * S), owner1);
+    } else {
+      *next = ~0ull;
     }
-    const uint64_t m = __shfl_sync(FULL, x, pos / S);
-    *next = n > 1 ? __shfl_sync(FULL, y, (pos + 1) / S) : ~0ull;
+    const bool mine = lane == owner;
+#pragma unroll
+    for (int j = 0; j < S; ++j) v[j] = (mine && j == r) ? 0ull : v[j];
     return m;
   }
 

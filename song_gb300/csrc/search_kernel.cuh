@@ -319,7 +319,9 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
   qn = 1;
   vh.add(0u, lane);
   int hops = 0, evals = 1;
-  int version = 0;  // number of changes of the top-k set (LEARNED)
+  int version = 0;           // number of changes of the top-k set (LEARNED)
+  int last_change = 0;       // hop of the latest change (LEARNED)
+  uint64_t kth_key = ~0ull;  // k-th smallest key of T, ~0 while tn < k (LEARNED)
 
   while (qn > 0) {
     // :186-193 pop the minimum, drop it from the visited hash.
@@ -334,8 +336,12 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
     // :191 finish test (<=) against the list maximum.
     if (tn == pq && key_dist(T.max()) <= key_dist(now)) break;
     ++hops;
-    if (LEARNED && trace) {  // does `now` enter the current top-k?
-      if (tn < k || now < T.at(C - tn + k - 1, lane)) ++version;
+    // LEARNED: does `now` enter the current top-k?  (Only such an entry
+    // changes the k-th key: T drops its maximum, never a top-k key.)
+    const bool enters = LEARNED && now < kth_key;
+    if (enters) {
+      ++version;
+      last_change = hops;
     }
     // :198-210 move it to the top-pq list (when full, `now` is below the
     // list maximum, which is the one dropped).
@@ -349,6 +355,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       vh.add(now_id, lane);
       vh.del(key_id(ev), lane);
     }
+    if (enters && tn >= k) kth_key = T.at(C - tn + k - 1, lane);
     // :211-224 neighbours not in the visited hash, in row order.
     const int deg = static_cast<int>(__shfl_sync(FULL, a, 0));
     const bool isnb = lane >= 1 && lane <= deg;
@@ -396,12 +403,11 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       const bool check = p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= k;
       if (trace || check) {
       // Per-hop state: hop count, k-th and best distance, queue-head gap,
-      // distance evaluations.  Distances enter through scale-free, bounded
-      // quantities: the progress span d0 - best, the top-k spread and the
-      // queue-head gap relative to that span (signed log), and the
-      // progress relative to |d0| + |best|.
-      const int kk = min(k, tn);
-      const float kth = key_float(T.at(C - tn + kk - 1, lane));
+      // hops since the top-k last changed, distance evaluations.  Distances
+      // enter through scale-free, bounded quantities: the top-k spread and
+      // the queue-head gap relative to the progress span d0 - best (signed
+      // logs).
+      const float kth = key_float(tn >= k ? kth_key : T.max());
       const float best = key_float(T.at(C - tn, lane));
       const float head = nk != ~0ull ? key_float(nk) : kth;
       const float span = fabsf(d0 - best) + 1e-6f * (fabsf(d0) + fabsf(best)) + 1e-30f;
@@ -410,7 +416,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       float f[MLP_IN];
       f[0] = __log2f(1.0f + static_cast<float>(hops)) * 0.1f;
       f[1] = copysignf(log1pf(fabsf(r1)), r1);
-      f[2] = (d0 - best) / (fabsf(d0) + fabsf(best) + 1e-30f);
+      f[2] = __log2f(1.0f + static_cast<float>(hops - last_change)) * 0.1f;
       f[3] = copysignf(log1pf(fabsf(r3)), r3);
       f[4] = __log2f(1.0f + static_cast<float>(evals)) * 0.1f;
       if (trace && hops <= p.trace_hops && lane < TRACE_FIELDS) {

@@ -83,3 +83,36 @@ def test_learned_kernel_without_exit_matches_exact_visited_oracle(song, oracle, 
                 o_ids, o_hops, o_evals, _ = ox.kernel_search(g["queries"], pq, oracle.MODE_LEX_EXACT)
                 assert np.array_equal(ids, o_ids), (name, storage, pq)
                 assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
+
+
+def test_trace_features_match_oracle(song, oracle):
+    """Per-hop features and top-k change counts traced by the learned kernel
+    equal the oracle's restatement (orc_kernel_search_trace): counts and hop
+    numbers exactly, features to FP32 rounding (the kernel's log2 is the fast
+    hardware approximation)."""
+    import torch
+    from conftest import load_golden
+    for name in ("l2_s5_d32", "cos_s4_d16"):
+        g = load_golden(name)
+        shift, metric = int(g["shift"]), int(g["metric"])
+        ox = oracle.OracleIndex(g["data"], g["graph"], shift, metric)
+        q = g["queries"][:48]
+        nq, th = q.shape[0], 512
+        with song.Index(g["graph"], g["data"], shift, metric) as ix:
+            for pq, k in ((100, 10), (40, 1)):
+                dq = torch.from_numpy(np.ascontiguousarray(q)).cuda()
+                tr = torch.zeros(nq * th * 6, dtype=torch.float32, device="cuda")
+                fin = torch.zeros(nq * 2, dtype=torch.int32, device="cuda")
+                out = torch.empty((nq, k), dtype=torch.int64, device="cuda")
+                s = torch.cuda.current_stream()
+                ix.trace_device(dq.data_ptr(), nq, pq, k, th, tr.data_ptr(), fin.data_ptr(), out.data_ptr(),
+                                stream=s.cuda_stream)
+                s.synchronize()
+                tr = tr.view(nq, th, 6).cpu().numpy()
+                fin = fin.view(nq, 2).cpu().numpy()
+                for i in range(nq):
+                    otr, ofin, oids, _, _ = ox.kernel_search_trace(q[i], pq, k, th)
+                    n = otr.shape[0]
+                    assert fin[i, 0] == ofin and fin[i, 1] == n, (name, pq, i)
+                    assert np.array_equal(tr[i, :n, 5], otr[:, 5])
+                    np.testing.assert_allclose(tr[i, :n, :5], otr[:, :5], rtol=2e-5, atol=2e-6)

@@ -110,3 +110,22 @@ def test_fma_probe_separates_contraction(oracle):
         nf, *_ = ox.kernel_search(z["queries"][i:i + 1], int(z["pq"]), oracle.MODE_REF, use_fma=False)
         assert np.array_equal(f[0], z["fma_ids"][i]) and np.array_equal(nf[0], z["nofma_ids"][i])
         assert not np.array_equal(f[0], nf[0])
+
+
+@pytest.mark.parametrize("name", ["l2_s5_d32", "cos_s4_d16"])
+def test_trace_is_consistent_with_the_search(oracle, name):
+    """The oracle's per-hop trace runs the same search (ids, hops, evals) and
+    its top-k change count only grows, ending at the final count; the hop
+    feature counts hops and the stagnation feature restarts at each change."""
+    g = load_golden(name)
+    ox = oracle.OracleIndex(g["data"], g["graph"], int(g["shift"]), int(g["metric"]))
+    q = g["queries"][:16]
+    ids, hops, evals, _ = ox.kernel_search(q, 100, oracle.MODE_LEX_EXACT)
+    for i in range(q.shape[0]):
+        tr, fin, out, h, e = ox.kernel_search_trace(q[i], 100, 10, 4096)
+        assert np.array_equal(out, ids[i]) and h == hops[i] and e == evals[i]
+        assert tr.shape[0] == h and tr[-1, 5] == fin and np.all(np.diff(tr[:, 5]) >= 0)
+        assert np.allclose(2.0 ** (tr[:, 0] * 10.0) - 1.0, np.arange(1, h + 1), atol=1e-3)
+        stag = np.rint(2.0 ** (tr[:, 2] * 10.0) - 1.0)
+        changed = np.concatenate([[True], np.diff(tr[:, 5]) > 0])
+        assert np.all(stag[changed] == 0) and np.all(stag[~changed] > 0)
