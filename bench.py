@@ -60,10 +60,11 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cache", default=os.environ.get("SONG_CACHE", "/tmp/song_gb300_cache"))
     p.add_argument("--curve", action="store_true", help="time every pq of the sweep (recall/throughput curve)")
-    p.add_argument("--mode", choices=["best", "learned", "plain", "precision", "serve"], default="best",
+    p.add_argument("--mode", choices=["best", "learned", "plain", "precision", "serve", "build"], default="best",
                    help="best: measure the plain FP32 search and the learned early exit + BF16 (+FP32 rerank) "
                         "and report the faster at the recall target; learned / plain: that path only; "
-                        "precision: storage error and recall table; serve: Poisson request stream")
+                        "precision: storage error and recall table; serve: Poisson request stream; "
+                        "build: graph construction, GPU searches vs the CPU builder")
     p.add_argument("--serve-rate", type=float, default=20000.0, help="mean offered queries/s (serve)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="length of each request stream (serve)")
     p.add_argument("--rerank", type=int, default=100, help="FP32 re-ranked candidates (BF16 path)")
@@ -466,6 +467,55 @@ def run_serve(args, torch, local):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# build: graph construction with the searches on the GPU vs on host threads
+# ---------------------------------------------------------------------------
+
+def run_build(args, torch, local):
+    """Builds the workload's degree-32 graph with the CPU batch-parallel
+    builder (all host threads) and with the GPU builder (searches on the
+    GPU, edge updates on the host threads); the graphs must be identical."""
+    import hashlib
+    import song_gb300 as S
+    from song_gb300 import datasets as D
+    w = D.WORKLOADS[args.workload]
+    data = D.base_vectors(w)
+    nt = os.cpu_count() or 1
+    bargs = (data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150)
+    S.graph_build_gpu(data[:2000], w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
+                      batch_div=args.build_div, device=local)  # context and module load
+    t = time.perf_counter()
+    g_gpu = S.graph_build_gpu(*bargs, batch_div=args.build_div, device=local, nthreads=nt)
+    gpu_s = time.perf_counter() - t
+    log("[build] GPU builder %.2fs" % gpu_s)
+    t = time.perf_counter()
+    g_cpu = S.graph_build(*bargs, batch_div=args.build_div, nthreads=nt)
+    cpu_s = time.perf_counter() - t
+    log("[build] CPU builder %.2fs on %d threads" % (cpu_s, nt))
+    same = bool(np.array_equal(g_gpu, g_cpu))
+    assert same, "GPU and CPU builders disagree"
+    nb, a = 0, 0
+    while a < w.n:
+        a += max(1, a // args.build_div)
+        nb += 1
+    line = {"metric": "seconds to build the graph, %s (shift %d, SEARCH_DEGREE %d, budget 150, batch div %d)"
+                      % (w.name, w.shift, w.search_degree, args.build_div),
+            "value": round(gpu_s, 3), "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 data, f64 distance sums (the reference builder's arithmetic)",
+            "data": "synthetic (seeded Gaussian mixture)",
+            "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric,
+                       "graphs_identical": same, "graph_md5": hashlib.md5(g_gpu.tobytes()).hexdigest(),
+                       "batches": nb, "speedup_vs_cpu_builder": round(cpu_s / gpu_s, 2)},
+            "cpu_baseline": {"value": round(cpu_s, 3), "unit": "s", "cores": nt, "kind": "port",
+                             "sample": "the whole build (this project's restatement of the reference builder, "
+                                       "batch-parallel, row-parallel edge updates)"},
+            "e2e": {"value": round(gpu_s, 3), "unit": "s", "h2d_bytes_per_step": int(data.nbytes),
+                    "d2h_bytes_per_step": None},
+            "gpu_launches": 2 * nb}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -487,6 +537,9 @@ def main():
         return
     if args.mode == "serve":
         run_serve(args, torch, local)
+        return
+    if args.mode == "build":
+        run_build(args, torch, local)
         return
 
     def barrier():

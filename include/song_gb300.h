@@ -121,6 +121,14 @@ int song_graph_build(const float *data, uint64_t n, int dim, int metric, int shi
                      int search_degree, int fixed_degree, int budget, int batch_div, int nthreads,
                      uint64_t *graph_out);
 
+/* The same construction with each batch's searches (graph.h:169-216) on GPU
+ * `device`, one warp per new vertex, and the edge updates on nthreads host
+ * threads: graph_out equals song_graph_build's for the same arguments, bit
+ * for bit.  budget <= 1024, n < 2^32 - 1. */
+int song_graph_build_gpu(const float *data, uint64_t n, int dim, int metric, int shift,
+                         int search_degree, int fixed_degree, int budget, int batch_div, int device,
+                         int nthreads, uint64_t *graph_out);
+
 /* Low-precision storage (BF16 / FP8): number of the best final candidates
  * re-ranked with exact FP32 distances before the first k are returned.
  * -1 (default) = all pq, 0 = none (results in the storage's precision).

@@ -31,7 +31,7 @@ NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 EXPORTED = [
     "song_status_string", "song_last_error", "song_index_create", "song_index_load",
     "song_index_free", "song_index_info", "song_search", "song_search_device",
-    "song_astar_search_batch", "song_graph_build", "song_debug_fixhash", "song_search_noalloc",
+    "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_debug_fixhash", "song_search_noalloc",
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
     "song_index_set_hop_limit", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
@@ -85,6 +85,8 @@ def load_library():
     L.song_astar_search_batch.argtypes = [P, i32, i32, P, P, P, i32, u64, i32, i32]
     L.song_graph_build.restype = i32
     L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
+    L.song_graph_build_gpu.restype = i32
+    L.song_graph_build_gpu.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, i32, P]
     L.song_index_set_rerank.restype = i32
     L.song_index_set_rerank.argtypes = [P, i32]
     L.song_index_rows.restype = i32
@@ -282,6 +284,19 @@ def graph_build(data, metric, shift=5, search_degree=15, fixed_degree=31, budget
     _check(load_library().song_graph_build(_ptr(data), n, dim, _metric(metric), shift, search_degree,
                                            fixed_degree, budget, batch_div,
                                            nthreads or os.cpu_count() or 1, _ptr(out)))
+    return out
+
+
+def graph_build_gpu(data, metric, shift=5, search_degree=15, fixed_degree=31, budget=150,
+                    batch_div=64, device=0, nthreads=None):
+    """graph_build with the searches of every batch on the GPU; the same graph
+    bit for bit."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    n, dim = data.shape
+    out = np.empty(n << shift, dtype=np.uint64)
+    _check(load_library().song_graph_build_gpu(_ptr(data), n, dim, _metric(metric), shift, search_degree,
+                                               fixed_degree, budget, batch_div, device,
+                                               nthreads or os.cpu_count() or 1, _ptr(out)))
     return out
 
 

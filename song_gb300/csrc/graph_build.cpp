@@ -16,9 +16,17 @@
 // reference's graph exactly.  batch_div > 0 inserts them in batches of
 // max(1, inserted / batch_div): the searches of one batch run in parallel
 // against the graph as it stood before the batch, then the batch's edges are
-// applied one vertex at a time in id order.  The result is deterministic for
-// a given batch_div (independent of the thread count) but is not the
-// sequential graph.
+// applied as if one vertex at a time in id order.  The result is
+// deterministic for a given batch_div (independent of the thread count) but
+// is not the sequential graph.
+//
+// Applying a batch in parallel is exact: a batch's vertices only add reverse
+// edges to rows of vertices inserted before the batch, a row's updates
+// depend on nothing but that row, and each row receives its updates in
+// vertex-id order, as the sequential loop would give them.
+//
+// The searches of a batch can also run on the GPU (graph_build_gpu.cu, the
+// same search restated exactly); this file then only applies the edges.
 //
 // Distances are the reference's CPU ones (data.h:28-62): float products
 // accumulated in double; cosine divides by both squared norms kept in float.
@@ -30,6 +38,7 @@
 #include <thread>
 #include <vector>
 
+#include "graph_build.h"
 #include "song_gb300.h"
 
 namespace {
@@ -125,6 +134,63 @@ struct Builder {
       if (edges[off] == (uint64_t)fixed_degree) rank_edges(off);
     } else {
       rank_and_switch(v, u);
+    }
+  }
+
+  // Edges of the new vertices a..e-1 (nb(v): its search result, ascending),
+  // row-parallel over nthreads; the rows changed are appended to *touched.
+  template <class NB>
+  void apply_batch(uint64_t a, uint64_t e, NB nb, int nthreads, std::vector<uint64_t> *touched) {
+    const uint64_t m = e - a;
+    std::vector<std::pair<uint64_t, uint64_t>> upd;  // (target row, new vertex)
+    for (uint64_t v = a; v < e; ++v) {
+      const uint64_t *ids;
+      int cnt;
+      nb(v, &ids, &cnt);
+      const int num = std::min<int>(search_degree, cnt);
+      for (int i = 0; i < num; ++i) upd.push_back({ids[i], v});
+    }
+    std::sort(upd.begin(), upd.end());
+    std::vector<size_t> starts;  // one group per distinct target row
+    for (size_t i = 0; i < upd.size(); ++i)
+      if (i == 0 || upd[i].first != upd[i - 1].first) starts.push_back(i);
+    starts.push_back(upd.size());
+    const size_t groups = starts.size() - 1;
+    auto own = [&](uint64_t v) {
+      const uint64_t *ids;
+      int cnt;
+      nb(v, &ids, &cnt);
+      const int num = std::min<int>(search_degree, cnt);
+      size_t off = (size_t)v << shift;
+      edges[off] = (uint64_t)num;
+      for (int i = 0; i < num; ++i) edges[off + i + 1] = ids[i];
+      rank_edges(off);
+    };
+    auto rev = [&](size_t g) {
+      for (size_t i = starts[g]; i < starts[g + 1]; ++i) add_edge(upd[i].first, upd[i].second);
+    };
+    const uint64_t work = m + groups;
+    int nt = (int)std::min<uint64_t>((uint64_t)std::max(1, nthreads), work / 16 + 1);
+    if (nt <= 1) {
+      for (uint64_t v = a; v < e; ++v) own(v);
+      for (size_t g = 0; g < groups; ++g) rev(g);
+    } else {
+      std::atomic<uint64_t> next(0);
+      auto worker = [&]() {
+        for (;;) {
+          uint64_t i = next.fetch_add(1);
+          if (i >= work) break;
+          if (i < m) own(a + i);
+          else rev((size_t)(i - m));
+        }
+      };
+      std::vector<std::thread> th;
+      for (int t = 0; t < nt; ++t) th.emplace_back(worker);
+      for (auto &x : th) x.join();
+    }
+    if (touched) {
+      for (uint64_t v = a; v < e; ++v) touched->push_back(v);
+      for (size_t g = 0; g < groups; ++g) touched->push_back(upd[starts[g]].first);
     }
   }
 
@@ -263,10 +329,62 @@ extern "C" int song_graph_build(const float *data, uint64_t n, int dim, int metr
         for (int t = 0; t < nt; ++t) th.emplace_back(work, t);
         for (auto &x : th) x.join();
       }
-      for (uint64_t v = a; v < e; ++v) b.apply(v, res[v - a]);
+      b.apply_batch(a, e, [&](uint64_t v, const uint64_t **ids, int *cnt) {
+        *ids = res[v - a].data();
+        *cnt = (int)res[v - a].size();
+      }, nthreads, nullptr);
       a = e;
     }
   }
   std::memcpy(graph_out, b.edges.data(), sizeof(uint64_t) * ((size_t)n << shift));
   return SONG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Interface for the GPU searches (graph_build.h)
+// ---------------------------------------------------------------------------
+
+namespace song {
+
+struct GraphBuilder {
+  Builder b;
+};
+
+GraphBuilder *graph_builder_create(const float *data, uint64_t n, int dim, int metric, int shift,
+                                   int search_degree, int fixed_degree, int budget) {
+  GraphBuilder *g = nullptr;
+  try {
+    g = new GraphBuilder();
+    Builder &b = g->b;
+    b.data = data;
+    b.n = n;
+    b.dim = dim;
+    b.metric = metric;
+    b.shift = shift;
+    b.search_degree = search_degree;
+    b.fixed_degree = fixed_degree;
+    b.budget = budget;
+    b.edges.assign((size_t)n << shift, 0);
+    b.edge_dist.assign((size_t)n << shift, 0.0);
+  } catch (...) {
+    delete g;
+    return nullptr;
+  }
+  return g;
+}
+
+void graph_builder_free(GraphBuilder *g) { delete g; }
+
+void graph_builder_apply(GraphBuilder *g, uint64_t a, uint64_t e, const uint32_t *ids, const int32_t *cnt,
+                         int ld, int nthreads, std::vector<uint64_t> *touched) {
+  std::vector<uint64_t> wide((size_t)(e - a) * (size_t)ld);
+  for (size_t i = 0; i < wide.size(); ++i) wide[i] = ids[i];
+  g->b.apply_batch(a, e, [&](uint64_t v, const uint64_t **p, int *c) {
+    *p = wide.data() + (size_t)(v - a) * (size_t)ld;
+    *c = cnt[v - a];
+  }, nthreads, touched);
+}
+
+const uint64_t *graph_builder_edges(const GraphBuilder *g) { return g->b.edges.data(); }
+
+}  // namespace song
