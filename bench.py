@@ -552,6 +552,7 @@ def main():
     from song_gb300 import datasets as D
     from song_gb300 import groundtruth as GT
     from song_gb300 import learned as LE
+    from song_gb300 import replicas as R
     S.load_library()
     w, data, queries, graph = load_workload(args, rank, barrier)
     nq, k = queries.shape[0], args.topk
@@ -630,12 +631,8 @@ def main():
     kernel_ms = timed_steps(torch, run, pq, args.steps, flush, stream)
     wall = time.perf_counter() - wall0
     barrier()
-    total_s = sum(kernel_ms) / 1000.0
-    if dist:
-        tt = torch.tensor([total_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_s = float(tt.item())
-    value = world * nq * args.steps / total_s
+    total_s = R.max_over_ranks(sum(kernel_ms) / 1000.0, dist, "cuda")
+    value = R.whole_job_rate(nq, args.steps, world, total_s)
 
     # e2e: host buffers through song_search (pinned query buffer)
     pinned = torch.empty((nq, w.dim), dtype=torch.float32, pin_memory=True)
@@ -656,12 +653,8 @@ def main():
         e2e_times.append(time.perf_counter() - t)
     clocks = sampler.stop()
     assert np.array_equal(out_host, ids), "e2e results differ from the device-buffer results"
-    e2e_s = sum(e2e_times)
-    if dist:
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e = world * nq * args.steps / e2e_s
+    e2e_s = R.max_over_ranks(sum(e2e_times), dist, "cuda")
+    e2e = R.whole_job_rate(nq, args.steps, world, e2e_s)
 
     # roofline: algorithmic bytes per launch / mean kernel time
     if mode == "learned":
