@@ -1,20 +1,26 @@
 // reg_queue.cuh -- a sorted array of (distance, id) keys held in the registers
-// of one warp.  Replaces the reference's serial min-max heap (smmh2.h) and
-// binary heap (bin_heap.h).
+// of one warp.  The search keeps its candidate queue (the reference's serial
+// min-max heap, smmh2.h) and its top-pq list (the binary heap, bin_heap.h) in
+// two of them.
 //
 // Layout: capacity C = 32*S positions, lane-blocked (lane l holds positions
-// l*S .. l*S+S-1 in v[0..S-1]), ascending, RIGHT-aligned: the n live keys sit
-// at positions C-n .. C-1 and every position left of them holds 0, a key
-// smaller than any real key (real keys carry order-preserving distance bits
+// l*S .. l*S+S-1 in v[0..S-1]), ascending.  Both lists use the WINDOW form:
+// positions C-pq .. C-1 always hold pq keys, the live keys first and then
+// "infinite" keys (~0); every position left of the window holds 0, smaller
+// than any real key (real keys carry order-preserving distance bits
 // >= 0x007fffff in their high word).  Consequences:
+//   * an insertion is always "insert and drop the window's maximum": keys not
+//     below the new key move one place right and an infinite key (or, when
+//     all pq are live, the real maximum) falls off -- one code path, per-slot
+//     compares and selects, one shuffle at the lane boundary;
 //   * the maximum is always at position C-1 (lane 31, v[S-1]): O(1);
-//   * inserting without eviction moves the smaller keys one place left,
-//     inserting with eviction of the maximum moves the larger keys one place
-//     right; neither needs the insertion position, only per-slot compares
-//     against the new key and one shuffle for the lane boundary;
-//   * removing the minimum (position C-n) is the only operation that touches
-//     a run-time position: a select tree reads it, one select pass clears it.
-// All operations are warp-uniform.
+//   * the minimum is at position C-pq; removing it shifts the window one
+//     place left and appends an infinite key;
+//   * reads at a run-time (warp-uniform) position are a binary tree of
+//     selects on the slot bits; nothing is indexed at run time, so the array
+//     never goes to local memory.
+// (insert_grow, the right-aligned form without a window, serves the FP32
+// re-rank of low-precision storage.)  All operations are warp-uniform.
 #pragma once
 
 #include <cstdint>
@@ -84,22 +90,20 @@ struct RegQueue {
     return t[0];
   }
 
-  // Remove the minimum of n >= 1 live keys; returns it, and the new minimum
-  // in *next (~0 if none is left).
-  __device__ __forceinline__ uint64_t pop_min(int n, int lane, uint64_t *next) {
-    const int pos = C - n;  // warp-uniform
-    const int owner = pos / S, r = pos - owner * S;
+  // Window form (positions start .. C-1 hold the keys, start warp-uniform):
+  // returns the key at start and shifts the window one place left, position
+  // C-1 receiving ~0; *next gets the new key at start.
+  __device__ __forceinline__ uint64_t pop_window(int start, int lane, uint64_t *next) {
+    const int owner = start / S, r = start - owner * S;
     const uint64_t m = __shfl_sync(FULL, slot(r), owner);
-    if (n > 1) {
-      const int pos1 = pos + 1;
-      const int owner1 = pos1 / S;
-      *next = __shfl_sync(FULL, slot(pos1 - owner1 * S), owner1);
-    } else {
-      *next = ~0ull;
-    }
-    const bool mine = lane == owner;
+    uint64_t nxt = __shfl_down_sync(FULL, v[0], 1);
+    if (lane == 31) nxt = ~0ull;
 #pragma unroll
-    for (int j = 0; j < S; ++j) v[j] = (mine && j == r) ? 0ull : v[j];
+    for (int j = 0; j < S; ++j) {
+      const uint64_t right = j + 1 < S ? v[j + 1] : nxt;
+      v[j] = (lane * S + j) >= start ? right : v[j];
+    }
+    *next = __shfl_sync(FULL, slot(r), owner);
     return m;
   }
 

@@ -315,7 +315,16 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
   int qn = 0, tn = 0;
   Q.clear();
   T.clear();
-  Q.insert_grow(make_key(d0, 0u), lane);
+  // T holds pq keys at all times: tn real ones (ascending, from position
+  // C - pq) followed by pq - tn "infinite" keys, so every insertion evicts
+  // the window's maximum (an infinite one while tn < pq).
+#pragma unroll
+  for (int j = 0; j < S; ++j) T.v[j] = (lane * S + j) >= C - pq ? ~0ull : 0ull;
+  // Q likewise holds pq keys: qn real ones from position C - pq, then
+  // infinite ones; a pop shifts the window one place left.
+#pragma unroll
+  for (int j = 0; j < S; ++j) Q.v[j] = (lane * S + j) >= C - pq ? ~0ull : 0ull;
+  Q.insert_evict(make_key(d0, 0u), lane);
   qn = 1;
   vh.add(0u, lane);
   int hops = 0, evals = 1;
@@ -326,7 +335,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
   while (qn > 0) {
     // :186-193 pop the minimum, drop it from the visited hash.
     uint64_t qh;  // queue minimum after the pop
-    const uint64_t now = Q.pop_min(qn, lane, &qh);
+    const uint64_t now = Q.pop_window(C - pq, lane, &qh);
     --qn;
     const uint32_t now_id = key_id(now);
     uint32_t a = a_next;
@@ -345,17 +354,14 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
     }
     // :198-210 move it to the top-pq list (when full, `now` is below the
     // list maximum, which is the one dropped).
-    if (tn < pq) {
-      T.insert_grow(now, lane);
-      ++tn;
-      vh.add(now_id, lane);
-    } else {
+    {
       const uint64_t ev = T.max();
       T.insert_evict(now, lane);
       vh.add(now_id, lane);
-      vh.del(key_id(ev), lane);
+      if (tn < pq) ++tn;
+      else vh.del(key_id(ev), lane);
     }
-    if (enters && tn >= k) kth_key = T.at(C - tn + k - 1, lane);
+    if (enters && tn >= k) kth_key = T.at(C - pq + k - 1, lane);
     // :211-224 neighbours not in the visited hash, in row order.
     const int deg = static_cast<int>(__shfl_sync(FULL, a, 0));
     const bool isnb = lane >= 1 && lane <= deg;
@@ -385,19 +391,16 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       const float d = __shfl_sync(FULL, cd, c);
       const uint32_t id = __shfl_sync(FULL, cid, c);
       const uint64_t key = make_key(d, id);
-      if (qn < pq) {
-        Q.insert_grow(key, lane);
-        ++qn;
-        vh.add(id, lane);
-      } else {
-        const uint64_t qmax = Q.max();
-        if (key_dist(qmax) < key_dist(key)) continue;
-        // inserted, then the larger of the two leaves (:315-320)
-        const uint64_t ev = key < qmax ? qmax : key;
-        Q.insert_evict(key, lane);
-        vh.add(id, lane);
-        vh.del(key_id(ev), lane);
-      }
+      // Below pq live keys the window's maximum is an infinite key, which
+      // leaves; at pq, the select-insert rule, then the larger of the key
+      // and the maximum leaves (:315-320).
+      const uint64_t qmax = Q.max();
+      if (qn >= pq && key_dist(qmax) < key_dist(key)) continue;
+      const uint64_t ev = key < qmax ? qmax : key;
+      Q.insert_evict(key, lane);
+      vh.add(id, lane);
+      if (qn < pq) ++qn;
+      else vh.del(key_id(ev), lane);
     }
     if (LEARNED) {
       const bool check = p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= k;
@@ -407,8 +410,8 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       // enter through scale-free, bounded quantities: the top-k spread and
       // the queue-head gap relative to the progress span d0 - best (signed
       // logs).
-      const float kth = key_float(tn >= k ? kth_key : T.max());
-      const float best = key_float(T.at(C - tn, lane));
+      const float kth = key_float(tn >= k ? kth_key : T.at(C - pq + tn - 1, lane));
+      const float best = key_float(T.at(C - pq, lane));
       const float head = nk != ~0ull ? key_float(nk) : kth;
       const float span = fabsf(d0 - best) + 1e-6f * (fabsf(d0) + fabsf(best)) + 1e-30f;
       const float r1 = (kth - best) / span;
@@ -440,7 +443,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       uint32_t ids[4];
       const int cnt = min(4, R - base);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) ids[i] = i < cnt ? key_id(T.at(C - tn + base + i, lane)) : 0u;
+      for (int i = 0; i < 4; ++i) ids[i] = i < cnt ? key_id(T.at(C - pq + base + i, lane)) : 0u;
       float d[4];
       fp32_distances4<METRIC>(p, w.qv, ids, cnt, d, lane);
 #pragma unroll
@@ -460,8 +463,8 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
     // :331-335 ascending ids; slots past the list length get UINT64_MAX.
 #pragma unroll
     for (int j = 0; j < S; ++j) {
-      const int r = T.rank_of(j, tn, lane);
-      if (r >= 0 && r < k) o[r] = static_cast<uint64_t>(key_id(T.v[j]));
+      const int r = T.rank_of(j, pq, lane);
+      if (r >= 0 && r < k && r < tn) o[r] = static_cast<uint64_t>(key_id(T.v[j]));
     }
     for (int i = tn + lane; i < k; i += 32) o[i] = ~0ull;
   }
