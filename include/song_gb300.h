@@ -161,6 +161,16 @@ int song_index_set_early_exit(song_index *index, const float *weights, float thr
  * in the reference.  F32 and BF16 storage. */
 int song_index_set_hop_limit(song_index *index, int max_hops);
 
+/* Entry points (warp_astar_accelerator.h:173 always starts at vertex 0, which
+ * stays the default).  With count > 0 entry vertex ids, every query of
+ * song_search, song_search_device and song_search_trace_device starts at the
+ * entry nearest to it (the search's own distance on the FP32 rows, ties to the
+ * smaller id), chosen on the GPU before the search; the search itself is
+ * unchanged.  count = 0 restores vertex 0.  song_search_noalloc and the
+ * server always start at vertex 0. */
+#define SONG_MAX_ENTRIES 65536
+int song_index_set_entries(song_index *index, const uint64_t *ids, int count);
+
 /* Training of the early-exit network (no counterpart in the reference), all
  * buffers on the device, ordered on `stream`: x n x 5 features, y n labels
  * (0/1), w n sample weights or NULL, perm epochs x n sample indices or NULL

@@ -468,8 +468,8 @@ static void trace_hop(ktrace *tr, const kscratch *s, int qn, int ts, float d0, i
   f[5] = (float)tr->version;
 }
 
-static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, int use_fma,
-                       kscratch *s, uint64_t *out, int32_t *hops_out, int32_t *evals_out,
+static int ksearch_one(const orc_index *ix, const float *qv, uint64_t start, int pq, int mode,
+                       int use_fma, kscratch *s, uint64_t *out, int32_t *hops_out, int32_t *evals_out,
                        evlog *L, ktrace *tr) {
   const int cap = 8 * pq; /* FixHash<int, TOPK*4*2>, warp_astar_accelerator.h:59-61 */
   const int shift = ix->shift;
@@ -487,16 +487,17 @@ static int ksearch_one(const orc_index *ix, const float *qv, int pq, int mode, i
   int hops = 0, evals = 0;
   int last_change = 0;
 
-  float d0 = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, 0), use_fma);
+  /* :173 the search starts at vertex 0; `start` generalises it (entry points) */
+  float d0 = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, start), use_fma);
   evals = 1;
   if (mode == ORC_MODE_REF) {
-    kp_t e = {(double)d0, 0};
+    kp_t e = {(double)d0, start};
     smmh_insert(s->q, &hs, e);
   } else {
-    lk_t e = {d0, 0, 0};
+    lk_t e = {d0, 0, start};
     lk_insert(s->lq, &qn, e);
   }
-  vs_add(&vs, 0);
+  vs_add(&vs, start);
 
   for (;;) {
     uint64_t now_id;
@@ -648,6 +649,7 @@ typedef struct {
   volatile int err;
   int k;
   int32_t *explored;
+  const uint64_t *starts;
 } job_t;
 
 static int maxdeg_of(const orc_index *ix) { return (1 << ix->shift) - 1; }
@@ -664,8 +666,8 @@ static void *kworker(void *arg) {
     int i = __sync_fetch_and_add(&j->next, 1);
     if (i >= j->nq) break;
     int32_t h = 0, e = 0;
-    int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim, j->pq, j->mode,
-                         j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL, NULL);
+    int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim, j->starts ? j->starts[i] : 0,
+                         j->pq, j->mode, j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL, NULL);
     if (j->hops) j->hops[i] = h;
     if (j->evals) j->evals[i] = e;
     if (j->popped) j->popped[i] = ts;
@@ -698,6 +700,12 @@ static int run_pool(void *(*fn)(void *), job_t *j, int nthreads) {
 int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq, int mode,
                       int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                       int32_t *popped, int nthreads) {
+  return orc_kernel_search_from(ix, queries, nq, NULL, pq, mode, use_fma, out, hops, evals, popped, nthreads);
+}
+
+int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, const uint64_t *starts,
+                           int pq, int mode, int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
+                           int32_t *popped, int nthreads) {
   if (check_index(ix) || !queries || !out || nq < 0 || pq < 2 || pq > 4095) return -1;
   if (mode != ORC_MODE_REF && mode != ORC_MODE_LEX && mode != ORC_MODE_LEX_EXACT) return -1;
   job_t j;
@@ -712,6 +720,10 @@ int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq,
   j.hops = hops;
   j.evals = evals;
   j.popped = popped;
+  j.starts = starts;
+  if (starts)
+    for (int i = 0; i < nq; ++i)
+      if (starts[i] >= ix->n) return -1;
   return run_pool(kworker, &j, nthreads);
 }
 
@@ -724,7 +736,7 @@ int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int m
     return -1;
   }
   evlog L = {log, cap, 0};
-  ksearch_one(ix, query, pq, mode, use_fma, &s, out, NULL, NULL, &L, NULL);
+  ksearch_one(ix, query, 0, pq, mode, use_fma, &s, out, NULL, NULL, &L, NULL);
   if (n_events) *n_events = L.n;
   kscratch_free(&s);
   return 0;
@@ -742,7 +754,7 @@ int orc_kernel_search_trace(const orc_index *ix, const float *query, int pq, int
     return -1;
   }
   ktrace tr = {k, trace_hops, trace, 0, 0};
-  ksearch_one(ix, query, pq, mode, use_fma, &s, out, hops, evals, NULL, &tr);
+  ksearch_one(ix, query, 0, pq, mode, use_fma, &s, out, hops, evals, NULL, &tr);
   if (final_version) *final_version = tr.version;
   if (traced) *traced = tr.traced;
   kscratch_free(&s);
@@ -921,4 +933,25 @@ int orc_cpu_search(const orc_index *ix, const float *queries, int nq, int k, uin
   j.out = out;
   j.explored = explored;
   return run_pool(cworker, &j, nthreads);
+}
+
+int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
+                      int use_fma, uint64_t *starts) {
+  if (check_index(ix) || !queries || !entries || !starts || ne < 1) return -1;
+  for (int e = 0; e < ne; ++e)
+    if (entries[e] >= ix->n) return -1;
+  for (int i = 0; i < nq; ++i) {
+    const float *q = queries + (size_t)i * (size_t)ix->dim;
+    float best = 0.0f;
+    uint64_t bid = 0;
+    for (int e = 0; e < ne; ++e) {
+      float d = orc_kernel_distance(ix->metric, ix->dim, q, row(ix, entries[e]), use_fma);
+      if (e == 0 || d < best || (d == best && entries[e] < bid)) {
+        best = d;
+        bid = entries[e];
+      }
+    }
+    starts[i] = bid;
+  }
+  return 0;
 }

@@ -22,6 +22,7 @@ import numpy as np
 from .build import LIB_PATH
 
 SONG_OK, SONG_ERR_ARG, SONG_ERR_OOM, SONG_ERR_TIMEOUT, SONG_ERR_CUDA, SONG_ERR_IO = range(6)
+SONG_MAX_ENTRIES = 65536  # include/song_gb300.h
 METRICS = {"l2": 0, "ip": 1, "cos": 2}
 STORAGES = {"f32": 0, "bf16": 1, "fp8": 2}
 MAX_PQ = 1023
@@ -31,7 +32,7 @@ NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 EXPORTED = [
     "song_status_string", "song_last_error", "song_index_create", "song_index_load",
     "song_index_free", "song_index_info", "song_search", "song_search_device",
-    "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_debug_fixhash", "song_search_noalloc",
+    "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_index_set_entries", "song_debug_fixhash", "song_search_noalloc",
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
     "song_index_set_hop_limit", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
@@ -85,6 +86,8 @@ def load_library():
     L.song_astar_search_batch.argtypes = [P, i32, i32, P, P, P, i32, u64, i32, i32]
     L.song_graph_build.restype = i32
     L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
+    L.song_index_set_entries.restype = i32
+    L.song_index_set_entries.argtypes = [P, P, i32]
     L.song_graph_build_gpu.restype = i32
     L.song_graph_build_gpu.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, i32, P]
     L.song_index_set_rerank.restype = i32
@@ -212,6 +215,13 @@ class Index:
             raise ValueError("expected %d weights" % MLP_PARAMS)
         _check(load_library().song_index_set_early_exit(self._h, _ptr(w), float(threshold), int(min_hops), int(every)))
 
+    def set_entries(self, ids):
+        """Entry points: each query starts at the nearest of these vertices
+        (None or empty: vertex 0, the reference's start)."""
+        e = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint64)
+        _check(load_library().song_index_set_entries(self._h, _ptr(e) if e is not None and e.size else None,
+                                                     0 if e is None else int(e.size)))
+
     def set_hop_limit(self, max_hops):
         """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""
         _check(load_library().song_index_set_hop_limit(self._h, int(max_hops)))
@@ -285,6 +295,12 @@ def graph_build(data, metric, shift=5, search_degree=15, fixed_degree=31, budget
                                            fixed_degree, budget, batch_div,
                                            nthreads or os.cpu_count() or 1, _ptr(out)))
     return out
+
+
+def sample_entries(n, count=4096, seed=11):
+    """count distinct vertex ids drawn uniformly from 0..n-1 (seeded), sorted."""
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, min(count, n), replace=False)).astype(np.uint64)
 
 
 def graph_build_gpu(data, metric, shift=5, search_degree=15, fixed_degree=31, budget=150,

@@ -99,6 +99,9 @@ void release(song_index *ix) {
   cudaFree(ix->d_q);
   cudaFree(ix->d_out);
   cudaFree(ix->d_stats);
+  cudaFree(ix->d_entry_ids);
+  cudaFree(ix->d_entry_rows);
+  cudaFree(ix->d_starts);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;
 }
@@ -116,6 +119,8 @@ int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_
   c.counter = ix->d_counter;
   c.error = ix->d_error;
   song::apply_index_settings(ix, c);
+  int rc = song::prepare_starts(ix, c, s);
+  if (rc != SONG_OK) return rc;
   SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
   int e = song::launch_search(ix->dx, c, s);
   if (e == -1) return fail(SONG_ERR_ARG, "unsupported search shape");
@@ -500,6 +505,8 @@ int song_search_trace_device(song_index *ix, const float *d_queries, int nq, int
   c.trace = d_trace;
   c.trace_hops = trace_hops;
   c.trace_final = d_final;
+  rc = song::prepare_starts(ix, c, s);
+  if (rc != SONG_OK) return rc;
   SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
   int e = song::launch_search(ix->dx, c, s);
   if (e == -1) return fail(SONG_ERR_ARG, "unsupported search shape");

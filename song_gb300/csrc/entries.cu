@@ -1,0 +1,232 @@
+// entries.cu -- entry points: each query starts its search at the nearest of a
+// set of entry vertices instead of vertex 0.
+//
+// The reference always starts at vertex 0 (warp_astar_accelerator.h:173, and
+// graph.h:176 with its random start commented out); that stays the default.
+// With entries set (song_index_set_entries), a pre-pass picks for every query
+// the entry with the smallest search distance, ties to the smaller id, and
+// the search starts there.  Nothing else in the search changes.
+//
+// The distance is the search kernel's, bit for bit, on the FP32 rows: lane l
+// of the search sums dims l, l+32, ... with fused multiply-adds and the 32
+// partial sums meet in an xor butterfly (16, 8, 4, 2, 1).  Here one thread
+// computes a whole distance: it keeps the 32 partial sums, adds each element
+// to the partial of its lane in dimension order, and then adds them in the
+// butterfly's pairs, which gives every lane's (identical) result.  The entry
+// rows are copied once into a contiguous block, which stays in L2.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "internal.h"
+#include "song_gb300.h"
+
+namespace song {
+namespace {
+
+// One warp serves QB queries; lane e takes entries e, e+32, ... and reads
+// each entry row once, in 16-byte pieces, for all QB queries.  Rows and the
+// staged queries are zero-padded to dpad (a multiple of 4) floats: a padded
+// element adds fma(0, 0, t) = t, leaving every partial sum exactly as the
+// search leaves it.
+template <int METRIC, int QB>
+__global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries, int nq, int dim, int dpad,
+                                                            const float *entry_rows, const uint32_t *entry_ids,
+                                                            int n_entries, uint32_t *starts) {
+  extern __shared__ float4 qs4[];  // (blockDim / 32) * QB query rows of dpad floats
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int q0 = (blockIdx.x * (blockDim.x >> 5) + wib) * QB;
+  if (q0 >= nq) return;  // whole warps leave together
+  const int d4 = dpad >> 2;
+  float *qw = reinterpret_cast<float *>(qs4) + static_cast<size_t>(wib) * QB * dpad;
+  for (int b = 0; b < QB; ++b)
+    for (int j = lane; j < dpad; j += 32)
+      qw[b * dpad + j] = (q0 + b < nq && j < dim) ? queries[static_cast<size_t>(q0 + b) * dim + j] : 0.0f;
+  __syncwarp();
+  const float4 *q4 = reinterpret_cast<const float4 *>(qw);
+  float best[QB];
+  uint32_t best_id[QB];
+#pragma unroll
+  for (int b = 0; b < QB; ++b) {
+    best[b] = 0.0f;
+    best_id[b] = 0xffffffffu;
+  }
+  for (int e = lane; e < n_entries; e += 32) {
+    const float4 *x4 = reinterpret_cast<const float4 *>(entry_rows + static_cast<size_t>(e) * dpad);
+    float t[QB][32], l[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      l[i] = 0.0f;
+#pragma unroll
+      for (int b = 0; b < QB; ++b) t[b][i] = 0.0f;
+    }
+    for (int c0 = 0; c0 < d4; c0 += 8) {  // 32 dimensions: partial 4i + c takes dimension 4 (c0 + i) + c
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (c0 + i < d4) {
+          const float4 xv = __ldg(x4 + c0 + i);
+          const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+          for (int b = 0; b < QB; ++b) {
+            const float4 qv = q4[b * d4 + c0 + i];
+            const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (METRIC == SONG_METRIC_L2) {
+                const float d = __fsub_rn(qq[c], xs[c]);
+                t[b][4 * i + c] = __fmaf_rn(d, d, t[b][4 * i + c]);
+              } else {
+                t[b][4 * i + c] = __fmaf_rn(qq[c], xs[c], t[b][4 * i + c]);
+              }
+            }
+          }
+          if (METRIC == SONG_METRIC_COS) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) l[4 * i + c] = __fmaf_rn(xs[c], xs[c], l[4 * i + c]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+      for (int i = 0; i < off; ++i) {
+#pragma unroll
+        for (int b = 0; b < QB; ++b) t[b][i] = __fadd_rn(t[b][i], t[b][i + off]);
+        if (METRIC == SONG_METRIC_COS) l[i] = __fadd_rn(l[i], l[i + off]);
+      }
+    }
+    const uint32_t id = entry_ids[e];
+#pragma unroll
+    for (int b = 0; b < QB; ++b) {
+      float d;
+      if (METRIC == SONG_METRIC_L2) {
+        d = t[b][0];
+      } else if (METRIC == SONG_METRIC_IP) {
+        d = -t[b][0];
+      } else if (l[0] != 0.0f) {
+        const float sign = t[b][0] < 0.0f ? 1.0f : -1.0f;
+        d = __fdiv_rn(__fmul_rn(__fmul_rn(sign, t[b][0]), t[b][0]), l[0]);
+      } else {
+        d = 0.0f;
+      }
+      if (best_id[b] == 0xffffffffu || d < best[b] || (d == best[b] && id < best_id[b])) {
+        best[b] = d;
+        best_id[b] = id;
+      }
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < QB; ++b) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best[b], o);
+      const uint32_t oid = __shfl_xor_sync(0xffffffffu, best_id[b], o);
+      if (oid != 0xffffffffu && (best_id[b] == 0xffffffffu || ob < best[b] || (ob == best[b] && oid < best_id[b]))) {
+        best[b] = ob;
+        best_id[b] = oid;
+      }
+    }
+    if (lane == 0 && q0 + b < nq) starts[q0 + b] = best_id[b];
+  }
+}
+
+// Gathers the FP32 rows of the entries into a contiguous block.
+__global__ void gather_entry_rows_kernel(const float *rows, uint32_t row_floats, const uint32_t *ids, int n,
+                                         int dpad, float *out) {
+  const uint64_t total = static_cast<uint64_t>(n) * dpad;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t e = i / dpad;
+    out[i] = rows[static_cast<uint64_t>(ids[e]) * row_floats + (i - e * dpad)];
+  }
+}
+
+}  // namespace
+
+int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s) {
+  c.starts = nullptr;
+  if (ix->n_entries <= 0 || c.nq <= 0) return SONG_OK;
+  if (static_cast<size_t>(c.nq) > ix->cap_starts) {
+    if (ix->d_starts) cudaFree(ix->d_starts);
+    ix->d_starts = nullptr;
+    ix->cap_starts = 0;
+    cudaError_t e = cudaMalloc(&ix->d_starts, sizeof(uint32_t) * c.nq);
+    if (e != cudaSuccess) return fail(SONG_ERR_OOM, "entry starts: %s", cudaGetErrorString(e));
+    ix->cap_starts = static_cast<size_t>(c.nq);
+  }
+  const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
+  // warps per block: up to 8, within the default 48 KB of shared memory
+  const int per_warp = static_cast<int>(sizeof(float)) * dpad * (ix->dx.metric == SONG_METRIC_COS ? 1 : 2);
+  const int wpb = std::max(1, std::min(8, (48 * 1024) / per_warp));
+  switch (ix->dx.metric) {
+    case SONG_METRIC_L2:
+    case SONG_METRIC_IP: {
+      constexpr int QB = 2;
+      const size_t smem = sizeof(float) * dpad * wpb * QB;
+      const unsigned grid = static_cast<unsigned>((c.nq + wpb * QB - 1) / (wpb * QB));
+      if (ix->dx.metric == SONG_METRIC_L2)
+        nearest_entry_kernel<SONG_METRIC_L2, QB><<<grid, 32 * wpb, smem, s>>>(
+            c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ix->d_starts);
+      else
+        nearest_entry_kernel<SONG_METRIC_IP, QB><<<grid, 32 * wpb, smem, s>>>(
+            c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ix->d_starts);
+      break;
+    }
+    default: {
+      const size_t smem = sizeof(float) * dpad * wpb;
+      const unsigned grid = static_cast<unsigned>((c.nq + wpb - 1) / wpb);
+      nearest_entry_kernel<SONG_METRIC_COS, 1><<<grid, 32 * wpb, smem, s>>>(
+          c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ix->d_starts);
+      break;
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "entry launch: %s", cudaGetErrorString(e));
+  c.starts = ix->d_starts;
+  return SONG_OK;
+}
+
+}  // namespace song
+
+extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int count) {
+  using namespace song;
+  clear_error();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (count < 0 || count > SONG_MAX_ENTRIES) return fail(SONG_ERR_ARG, "entry count must be 0..%d", SONG_MAX_ENTRIES);
+  if (count > 0 && !ids) return fail(SONG_ERR_ARG, "null entry ids");
+  std::vector<uint32_t> h(static_cast<size_t>(count));
+  for (int i = 0; i < count; ++i) {
+    if (ids[i] >= ix->dx.n) return fail(SONG_ERR_ARG, "entry %d: id %llu >= n", i, (unsigned long long)ids[i]);
+    h[i] = static_cast<uint32_t>(ids[i]);
+  }
+  cudaError_t e = cudaSetDevice(ix->device);
+  if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  cudaFree(ix->d_entry_ids);
+  cudaFree(ix->d_entry_rows);
+  ix->d_entry_ids = nullptr;
+  ix->d_entry_rows = nullptr;
+  ix->n_entries = 0;
+  if (count == 0) return SONG_OK;
+  const int dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
+  e = cudaMalloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = cudaMalloc(&ix->d_entry_rows, sizeof(float) * count * static_cast<size_t>(dpad));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ix->d_entry_ids, h.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
+  if (e == cudaSuccess) {
+    gather_entry_rows_kernel<<<256, 256, 0, ix->stream>>>(ix->dx.rows_f32, static_cast<uint32_t>(dpad),
+                                                          ix->d_entry_ids, count, dpad, ix->d_entry_rows);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
+  if (e != cudaSuccess) {
+    cudaFree(ix->d_entry_ids);
+    cudaFree(ix->d_entry_rows);
+    ix->d_entry_ids = nullptr;
+    ix->d_entry_rows = nullptr;
+    return fail(e == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "entries: %s", cudaGetErrorString(e));
+  }
+  ix->n_entries = count;
+  return SONG_OK;
+}

@@ -42,6 +42,7 @@ struct SearchCall {
   float *trace = nullptr;          // per-hop features, nq x trace_hops x 6, or null
   int trace_hops = 0;
   int32_t *trace_final = nullptr;  // nq x 2: final top-k version, hops traced
+  const uint32_t *starts = nullptr;  // per-query start vertex (entry points), null = vertex 0
 };
 
 // Launch the plain search.  Returns a cudaError_t-compatible code (0 ok) or
@@ -90,5 +91,18 @@ struct song_index {
   size_t cap_out = 0;
   int32_t *d_stats = nullptr;
   size_t cap_stats = 0;
+  // entry points (song_index_set_entries): ids, their FP32 rows, per-call starts
+  uint32_t *d_entry_ids = nullptr;
+  float *d_entry_rows = nullptr;
+  int n_entries = 0;
+  uint32_t *d_starts = nullptr;
+  size_t cap_starts = 0;
   uint64_t device_bytes = 0;
 };
+
+namespace song {
+// Entry points: with entries set on the index, picks every query's start
+// vertex (entries.cu) on stream s and points c.starts at them; otherwise
+// leaves c.starts null.  Returns a SONG_* status.
+int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s);
+}  // namespace song

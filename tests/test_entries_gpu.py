@@ -1,0 +1,81 @@
+"""Entry points (song_index_set_entries): every query starts at its nearest
+entry vertex instead of vertex 0.  The entry choice and the search from it
+must equal the oracle's (orc_nearest_entry + orc_kernel_search_from) bit for
+bit, for F32 and BF16 storage and for the learned kernel with its exit off;
+clearing the entries restores the reference's start at vertex 0."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _entries(n, count, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, count, replace=False)).astype(np.uint64)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_search_from_nearest_entry_matches_oracle(song, oracle, name):
+    g = load_golden(name)
+    shift, metric = int(g["shift"]), int(g["metric"])
+    ox = oracle.OracleIndex(g["data"], g["graph"], shift, metric)
+    ent = _entries(g["data"].shape[0], 64, 5)
+    starts = ox.nearest_entry(g["queries"], ent)
+    assert len(set(starts.tolist())) > 1  # the queries do not all start at one vertex
+    with song.Index(g["graph"], g["data"], shift, metric) as ix:
+        ix.set_entries(ent)
+        for pq in (10, 50, 100):
+            ids, hops, evals = ix.search(g["queries"], pq, pq, stats=True)
+            o_ids, o_hops, o_evals, _ = ox.kernel_search_from(g["queries"], starts, pq, oracle.MODE_LEX)
+            assert np.array_equal(ids, o_ids), (name, pq)
+            assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
+        ix.set_entries(None)
+        ids = ix.search(g["queries"], 50, 50)
+        o_ids, _, _, _ = ox.kernel_search(g["queries"], 50, oracle.MODE_LEX)
+        assert np.array_equal(ids, o_ids)
+
+
+@pytest.mark.parametrize("storage", ["bf16"])
+def test_entries_with_low_precision_rows(song, oracle, storage):
+    g = load_golden("cos_s5_d26")
+    shift, metric = int(g["shift"]), int(g["metric"])
+    ent = _entries(g["data"].shape[0], 100, 6)
+    starts = oracle.OracleIndex(g["data"], g["graph"], shift, metric).nearest_entry(g["queries"], ent)
+    with song.Index(g["graph"], g["data"], shift, metric, storage=storage) as ix:
+        ix.set_rerank(0)
+        ix.set_entries(ent)
+        deq = song.dequantize_rows(ix.rows(), storage, g["data"].shape[1])
+        ox = oracle.OracleIndex(deq, g["graph"], shift, metric)
+        ids, hops, evals = ix.search(g["queries"], 60, 60, stats=True)
+        o_ids, o_hops, o_evals, _ = ox.kernel_search_from(g["queries"], starts, 60, oracle.MODE_LEX)
+        assert np.array_equal(ids, o_ids) and np.array_equal(hops, o_hops)
+
+
+def test_learned_kernel_from_entries_matches_exact_visited_oracle(song, oracle):
+    import torch
+    from song_gb300 import learned as LE
+    g = load_golden("l2_s5_d32")
+    shift, metric = int(g["shift"]), int(g["metric"])
+    ox = oracle.OracleIndex(g["data"], g["graph"], shift, metric)
+    ent = _entries(g["data"].shape[0], 50, 7)
+    starts = ox.nearest_entry(g["queries"], ent)
+    with song.Index(g["graph"], g["data"], shift, metric) as ix:
+        ix.set_entries(ent)
+        dq = torch.from_numpy(g["queries"]).cuda()
+        ids, hops, evals = LE.evaluate(ix, dq, 100, 100, max_hops=1 << 30)
+    o_ids, o_hops, o_evals, _ = ox.kernel_search_from(g["queries"], starts, 100, oracle.MODE_LEX_EXACT)
+    assert np.array_equal(ids, o_ids) and np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
+
+
+def test_entry_arguments_are_checked(song):
+    g = load_golden("ip_s5_d24")
+    n = g["data"].shape[0]
+    with song.Index(g["graph"], g["data"], int(g["shift"]), int(g["metric"])) as ix:
+        with pytest.raises(song.SongError):
+            ix.set_entries(np.array([0, n], dtype=np.uint64))
+        with pytest.raises(song.SongError):
+            ix.set_entries(np.zeros(song.SONG_MAX_ENTRIES + 1, dtype=np.uint64))
+        ix.set_entries(np.array([n - 1], dtype=np.uint64))  # a single entry is allowed
+        assert ix.search(g["queries"][:3], 20, 5).shape == (3, 5)
