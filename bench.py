@@ -603,11 +603,14 @@ def main():
     if mode == "learned":
         ix = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
         ix.set_rerank(args.rerank)
+        if args.entries > 0:  # the same entry points as the entries arm (traces start there too)
+            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10))
         run = Runner(ix, dq, k, stream)
         train_q = D.query_vectors(w, nq=args.train_queries, seed=D.SEED_TRAIN)
-        pq, model, lrec = pq32, None, 0.0
+        pq0 = min(pq32, ent["pq"]) if ent else pq32
+        pq, model, lrec = pq0, None, 0.0
         tried = []
-        for cand in [c for c in PQ_SWEEP + [1023] if c >= pq32][:3]:
+        for cand in [c for c in PQ_SWEEP + [1023] if c >= pq0][:3]:
             model = LE.fit(ix, train_q, cand, k, epochs=6, data=data, metric=w.metric,
                            recall_slack=args.recall_slack, log=log)
             ix.set_early_exit(model.params, model.threshold, model.min_hops, model.every)
@@ -736,7 +739,8 @@ def main():
             cpu = {"value": None, "error": repr(e)}
 
     if rank == 0:
-        desc = {"learned": "learned early exit + BF16 storage + FP32 rerank",
+        desc = {"learned": "learned early exit + BF16 storage + FP32 rerank"
+                           + (", from the nearest of %d entry vertices" % args.entries if args.entries > 0 else ""),
                 "entries": "FP32 search from the nearest of %d entry vertices" % args.entries,
                 "plain": "plain FP32 search"}[mode]
         line = {
