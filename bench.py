@@ -85,7 +85,7 @@ def parse_args():
 # workload
 # ---------------------------------------------------------------------------
 
-def load_workload(args, rank=0, barrier=None):
+def load_workload(args, rank=0, barrier=None, gpu_build=True):
     import song_gb300 as S
     from song_gb300 import datasets as D
     w = D.WORKLOADS[args.workload]
@@ -97,13 +97,21 @@ def load_workload(args, rank=0, barrier=None):
     os.makedirs(args.cache, exist_ok=True)
     gpath = os.path.join(args.cache, "%s.div%d.graph" % (w.name, args.build_div))
     if rank == 0 and not os.path.exists(gpath):
+        # The GPU builder writes the CPU builder's graph bit for bit
+        # (tests/test_graph_build_gpu.py), in a third of the time.
         t = time.time()
-        g = S.graph_build(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
-                          batch_div=args.build_div, nthreads=os.cpu_count())
+        if gpu_build:
+            g = S.graph_build_gpu(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
+                                  batch_div=args.build_div, device=int(os.environ.get("LOCAL_RANK", "0")),
+                                  nthreads=os.cpu_count())
+        else:
+            g = S.graph_build(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
+                              batch_div=args.build_div, nthreads=os.cpu_count())
         tmp = gpath + ".tmp%d" % os.getpid()
         g.tofile(tmp)
         os.replace(tmp, gpath)
-        log("[bench] graph built in %.1fs (batch_div %d, %d threads)" % (time.time() - t, args.build_div, os.cpu_count()))
+        log("[bench] graph built in %.1fs (%s builder, batch_div %d, %d threads)"
+            % (time.time() - t, "GPU" if gpu_build else "CPU", args.build_div, os.cpu_count()))
     if barrier:
         barrier()
     graph = np.fromfile(gpath, dtype=np.uint64)
@@ -233,7 +241,7 @@ def run_reference(args, rank, world):
         return
     from oracle import oracle as O
     O.build()
-    w, data, queries, graph = load_workload(args)
+    w, data, queries, graph = load_workload(args, gpu_build=False)
     from song_gb300 import groundtruth as GT
     sample = min(400, queries.shape[0])
     gt_ids, gt_kth = GT.exact_knn_fp64(data, queries[:sample], args.topk, w.metric, device="cpu")
@@ -348,6 +356,7 @@ def run_precision(args, torch, local):
     """Storage error of the F32/BF16/FP8 rows against FP64 on every exact
     top-k pair, and recall@k / queries/s per storage, rerank on/off, pq."""
     import song_gb300 as S
+    from song_gb300 import datasets as D
     from song_gb300 import groundtruth as GT
     w, data, queries, graph = load_workload(args)
     nq, k = queries.shape[0], args.topk
@@ -373,24 +382,30 @@ def run_precision(args, torch, local):
                            "pairs": int(rel.size)}
         log("[precision] %s distance error vs FP64 over exact top-%d pairs: %s" % (storage, k, errors[storage]))
         run = Runner(ix, dq, k, stream)
-        for rerank in ((0,) if storage == "f32" else (0, -1)):
-            if storage != "f32":
-                ix.set_rerank(rerank)
-            for pq in pqs:
-                run(pq, stats=True)
-                rec = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
-                for _ in range(2):
-                    run(pq)
-                ms = timed_steps(torch, run, pq, 3, flush, stream)
-                qps = nq / (statistics.median(ms) / 1000.0)
-                if storage == "f32":
-                    recall_f32[pq] = rec
-                row = {"storage": storage, "rerank": "all pq" if rerank == -1 else "none", "pq": pq,
-                       "recall_at_%d" % k: round(rec, 4), "recall_loss_vs_f32": round(recall_f32[pq] - rec, 4),
-                       "qps": round(qps, 1), "mean_hops": round(float(run.hops.float().mean().item()), 1),
-                       "mean_evals": round(float(run.evals.float().mean().item()), 1)}
-                table.append(row)
-                log("[precision] %s" % row)
+        starts = [("vertex 0", None)]
+        if args.entries > 0:
+            starts.append(("%d entries" % args.entries, S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10)))
+        for start, ents in starts:
+            ix.set_entries(ents)
+            for rerank in ((0,) if storage == "f32" else (0, -1)):
+                if storage != "f32":
+                    ix.set_rerank(rerank)
+                for pq in pqs:
+                    run(pq, stats=True)
+                    rec = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
+                    for _ in range(2):
+                        run(pq)
+                    ms = timed_steps(torch, run, pq, 3, flush, stream)
+                    qps = nq / (statistics.median(ms) / 1000.0)
+                    if storage == "f32":
+                        recall_f32[(start, pq)] = rec
+                    row = {"storage": storage, "rerank": "all pq" if rerank == -1 else "none", "start": start,
+                           "pq": pq, "recall_at_%d" % k: round(rec, 4),
+                           "recall_loss_vs_f32": round(recall_f32[(start, pq)] - rec, 4),
+                           "qps": round(qps, 1), "mean_hops": round(float(run.hops.float().mean().item()), 1),
+                           "mean_evals": round(float(run.evals.float().mean().item()), 1)}
+                    table.append(row)
+                    log("[precision] %s" % row)
         ix.free()
     # headline: the fastest configuration that loses at most 0.002 recall
     ok = [r for r in table if r["recall_loss_vs_f32"] <= 0.002]
