@@ -570,13 +570,18 @@ int launch_by_s(const Params &p, int S, cudaStream_t s) {
 
 template <int STORAGE, bool LEARNED>
 int launch_storage(const Params &p, int metric, int H, int S, cudaStream_t s) {
-  switch (metric * 2 + (H == 4 ? 1 : 0)) {
-    case 0: return launch_by_s<0, STORAGE, 2, LEARNED>(p, S, s);
-    case 1: return launch_by_s<0, STORAGE, 4, LEARNED>(p, S, s);
-    case 2: return launch_by_s<1, STORAGE, 2, LEARNED>(p, S, s);
-    case 3: return launch_by_s<1, STORAGE, 4, LEARNED>(p, S, s);
-    case 4: return launch_by_s<2, STORAGE, 2, LEARNED>(p, S, s);
-    case 5: return launch_by_s<2, STORAGE, 4, LEARNED>(p, S, s);
+  const int h = H == 1 ? 0 : (H == 2 ? 1 : (H == 4 ? 2 : -1));
+  if (h < 0) return -1;
+  switch (metric * 3 + h) {
+    case 0: return launch_by_s<0, STORAGE, 1, LEARNED>(p, S, s);
+    case 1: return launch_by_s<0, STORAGE, 2, LEARNED>(p, S, s);
+    case 2: return launch_by_s<0, STORAGE, 4, LEARNED>(p, S, s);
+    case 3: return launch_by_s<1, STORAGE, 1, LEARNED>(p, S, s);
+    case 4: return launch_by_s<1, STORAGE, 2, LEARNED>(p, S, s);
+    case 5: return launch_by_s<1, STORAGE, 4, LEARNED>(p, S, s);
+    case 6: return launch_by_s<2, STORAGE, 1, LEARNED>(p, S, s);
+    case 7: return launch_by_s<2, STORAGE, 2, LEARNED>(p, S, s);
+    case 8: return launch_by_s<2, STORAGE, 4, LEARNED>(p, S, s);
     default: return -1;
   }
 }
