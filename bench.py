@@ -69,6 +69,7 @@ def parse_args():
                         "precision: storage error and recall table; serve: Poisson request stream; "
                         "build: graph construction, GPU searches vs the CPU builder")
     p.add_argument("--entries", type=int, default=4096, help="entry vertices of the entries arm (sampled, seeded)")
+    p.add_argument("--starts", type=int, default=4, help="start vertices per query: its nearest entries")
     p.add_argument("--serve-rate", type=float, default=20000.0, help="mean offered queries/s (serve)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="length of each request stream (serve)")
     p.add_argument("--rerank", type=int, default=100, help="FP32 re-ranked candidates (BF16 path)")
@@ -384,9 +385,10 @@ def run_precision(args, torch, local):
         run = Runner(ix, dq, k, stream)
         starts = [("vertex 0", None)]
         if args.entries > 0:
-            starts.append(("%d entries" % args.entries, S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10)))
+            starts.append(("nearest %d of %d entries" % (args.starts, args.entries),
+                           S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10)))
         for start, ents in starts:
-            ix.set_entries(ents)
+            ix.set_entries(ents, starts=args.starts)
             for rerank in ((0,) if storage == "f32" else (0, -1)):
                 if storage != "f32":
                     ix.set_rerank(rerank)
@@ -600,7 +602,7 @@ def main():
     ent = None
     if args.mode in ("best", "entries") and args.entries > 0:
         ixe = S.Index(graph, data, w.shift, w.metric, device=local)
-        ixe.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10))
+        ixe.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10), starts=args.starts)
         rune = Runner(ixe, dq, k, stream)
         pqe, sweepe = (args.pq, []) if args.pq else sweep_pq(torch, rune, w, data, queries, gt_kth, k, args.recall,
                                                               args.curve, "fp32+entries")
@@ -608,7 +610,7 @@ def main():
         rece = GT.recall_tie_aware(rune.ids(), data, queries, gt_kth, w.metric, k)
         mse = timed_steps(torch, rune, pqe, max(3, args.steps // 2), flush, stream)
         ent = {"qps": round(nq / (statistics.median(mse) / 1000.0), 1), "pq": pqe, "recall_at_10": round(rece, 4),
-               "entries": args.entries, "kernel_ms_median": round(statistics.median(mse), 4),
+               "entries": args.entries, "starts_per_query": args.starts, "kernel_ms_median": round(statistics.median(mse), 4),
                "mean_hops": round(float(rune.hops.float().mean().item()), 2),
                "mean_evals": round(float(rune.evals.float().mean().item()), 2), "pq_sweep_recall_qps": sweepe}
         log("[bench] FP32 from entries: %s" % ent)
@@ -619,7 +621,7 @@ def main():
         ix = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
         ix.set_rerank(args.rerank)
         if args.entries > 0:  # the same entry points as the entries arm (traces start there too)
-            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10))
+            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10), starts=args.starts)
         run = Runner(ix, dq, k, stream)
         train_q = D.query_vectors(w, nq=args.train_queries, seed=D.SEED_TRAIN)
         pq0 = min(pq32, ent["pq"]) if ent else pq32
@@ -755,8 +757,9 @@ def main():
 
     if rank == 0:
         desc = {"learned": "learned early exit + BF16 storage + FP32 rerank"
-                           + (", from the nearest of %d entry vertices" % args.entries if args.entries > 0 else ""),
-                "entries": "FP32 search from the nearest of %d entry vertices" % args.entries,
+                           + (", from the nearest %d of %d entry vertices" % (args.starts, args.entries)
+                              if args.entries > 0 else ""),
+                "entries": "FP32 search from the nearest %d of %d entry vertices" % (args.starts, args.entries),
                 "plain": "plain FP32 search"}[mode]
         line = {
             "metric": "queries/s at recall@10>=%.2f, %s (%s)" % (args.recall, w.name, desc),

@@ -163,13 +163,16 @@ int song_index_set_hop_limit(song_index *index, int max_hops);
 
 /* Entry points (warp_astar_accelerator.h:173 always starts at vertex 0, which
  * stays the default).  With count > 0 entry vertex ids, every query of
- * song_search, song_search_device and song_search_trace_device starts at the
- * entry nearest to it (the search's own distance on the FP32 rows, ties to the
- * smaller id), chosen on the GPU before the search; the search itself is
- * unchanged.  count = 0 restores vertex 0.  song_search_noalloc and the
- * server always start at vertex 0. */
+ * song_search, song_search_device and song_search_trace_device starts from
+ * the `starts` entries nearest to it (the search's own distance on the FP32
+ * rows, ties to the smaller id), chosen on the GPU before the search: they
+ * enter the candidate queue and the visited set nearest first, and the search
+ * itself is unchanged.  1 <= starts <= min(SONG_MAX_STARTS, count) and
+ * starts <= pq.  count = 0 restores vertex 0.  song_search_noalloc and the
+ * server always start at vertex 0.  No counterpart in the reference. */
 #define SONG_MAX_ENTRIES 65536
-int song_index_set_entries(song_index *index, const uint64_t *ids, int count);
+#define SONG_MAX_STARTS 8
+int song_index_set_entries(song_index *index, const uint64_t *ids, int count, int starts);
 
 /* Training of the early-exit network (no counterpart in the reference), all
  * buffers on the device, ordered on `stream`: x n x 5 features, y n labels

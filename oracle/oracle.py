@@ -82,9 +82,9 @@ def lib():
         L.orc_classify.restype = i32
         L.orc_classify.argtypes = [P, i32, P, i32, P]
         L.orc_kernel_search_from.restype = i32
-        L.orc_kernel_search_from.argtypes = [P, P, i32, P, i32, i32, i32, P, P, P, P, i32]
+        L.orc_kernel_search_from.argtypes = [P, P, i32, P, i32, i32, i32, i32, P, P, P, P, i32]
         L.orc_nearest_entry.restype = i32
-        L.orc_nearest_entry.argtypes = [P, P, i32, P, i32, i32, P]
+        L.orc_nearest_entry.argtypes = [P, P, i32, P, i32, i32, i32, P]
         L.orc_kernel_search_trace.restype = i32
         L.orc_kernel_search_trace.argtypes = [P, P, i32, i32, i32, i32, i32, P, P, P, P, P, P]
         L.orc_cpu_search.restype = i32
@@ -141,28 +141,31 @@ class OracleIndex:
         return out, hops, evals, popped
 
     def kernel_search_from(self, queries, starts, pq, mode=MODE_LEX, use_fma=True, nthreads=None):
-        """kernel_search with query i starting at vertex starts[i]."""
+        """kernel_search with query i starting from the vertices starts[i]
+        (an nq-vector: one start each; nq x ns: ns starts each)."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         st = np.ascontiguousarray(starts, dtype=np.uint64)
+        ns = 1 if st.ndim == 1 else st.shape[1]
         nq = q.shape[0]
         out = np.empty((nq, pq), dtype=np.uint64)
         hops = np.empty(nq, dtype=np.int32)
         evals = np.empty(nq, dtype=np.int32)
         popped = np.empty(nq, dtype=np.int32)
-        rc = lib().orc_kernel_search_from(self.ref, _ptr(q), nq, _ptr(st), pq, mode, int(use_fma), _ptr(out),
+        rc = lib().orc_kernel_search_from(self.ref, _ptr(q), nq, _ptr(st), ns, pq, mode, int(use_fma), _ptr(out),
                                           _ptr(hops), _ptr(evals), _ptr(popped), nthreads or default_threads())
         if rc != 0:
             raise ValueError("orc_kernel_search_from failed")
         return out, hops, evals, popped
 
-    def nearest_entry(self, queries, entries, use_fma=True):
-        """Per query, the entry vertex nearest by the kernel's distance."""
+    def nearest_entry(self, queries, entries, ns=1, use_fma=True):
+        """Per query, the ns entry vertices nearest by the kernel's distance,
+        ascending (an nq-vector when ns == 1, else nq x ns)."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         e = np.ascontiguousarray(entries, dtype=np.uint64)
-        out = np.empty(q.shape[0], dtype=np.uint64)
-        if lib().orc_nearest_entry(self.ref, _ptr(q), q.shape[0], _ptr(e), e.size, int(use_fma), _ptr(out)) != 0:
+        out = np.empty((q.shape[0], ns), dtype=np.uint64)
+        if lib().orc_nearest_entry(self.ref, _ptr(q), q.shape[0], _ptr(e), e.size, ns, int(use_fma), _ptr(out)) != 0:
             raise ValueError("orc_nearest_entry failed")
-        return out
+        return out[:, 0].copy() if ns == 1 else out
 
     def kernel_search_log(self, query, pq, mode, use_fma=True, cap=1 << 18):
         q = np.ascontiguousarray(query, dtype=np.float32).reshape(-1)

@@ -468,9 +468,9 @@ static void trace_hop(ktrace *tr, const kscratch *s, int qn, int ts, float d0, i
   f[5] = (float)tr->version;
 }
 
-static int ksearch_one(const orc_index *ix, const float *qv, uint64_t start, int pq, int mode,
-                       int use_fma, kscratch *s, uint64_t *out, int32_t *hops_out, int32_t *evals_out,
-                       evlog *L, ktrace *tr) {
+static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *starts, int ns, int pq,
+                       int mode, int use_fma, kscratch *s, uint64_t *out, int32_t *hops_out,
+                       int32_t *evals_out, evlog *L, ktrace *tr) {
   const int cap = 8 * pq; /* FixHash<int, TOPK*4*2>, warp_astar_accelerator.h:59-61 */
   const int shift = ix->shift;
   int32_t *tab = s->tab;
@@ -487,17 +487,25 @@ static int ksearch_one(const orc_index *ix, const float *qv, uint64_t start, int
   int hops = 0, evals = 0;
   int last_change = 0;
 
-  /* :173 the search starts at vertex 0; `start` generalises it (entry points) */
-  float d0 = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, start), use_fma);
-  evals = 1;
-  if (mode == ORC_MODE_REF) {
-    kp_t e = {(double)d0, start};
-    smmh_insert(s->q, &hs, e);
-  } else {
-    lk_t e = {d0, 0, start};
-    lk_insert(s->lq, &qn, e);
+  /* :173 the search starts at vertex 0.  Entry points generalise it: the ns
+   * start vertices enter the queue (and the visited set) in order before the
+   * first pop; d0, the progress reference of the early-exit features, is the
+   * first start's distance. */
+  float d0 = 0.0f;
+  for (int si = 0; si < ns; ++si) {
+    const uint64_t start = starts[si];
+    const float d = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, start), use_fma);
+    if (si == 0) d0 = d;
+    if (mode == ORC_MODE_REF) {
+      kp_t e = {(double)d, start};
+      smmh_insert(s->q, &hs, e);
+    } else {
+      lk_t e = {d, 0, start};
+      lk_insert(s->lq, &qn, e);
+    }
+    vs_add(&vs, start);
   }
-  vs_add(&vs, start);
+  evals = ns;
 
   for (;;) {
     uint64_t now_id;
@@ -650,6 +658,7 @@ typedef struct {
   int k;
   int32_t *explored;
   const uint64_t *starts;
+  int ns;
 } job_t;
 
 static int maxdeg_of(const orc_index *ix) { return (1 << ix->shift) - 1; }
@@ -666,7 +675,9 @@ static void *kworker(void *arg) {
     int i = __sync_fetch_and_add(&j->next, 1);
     if (i >= j->nq) break;
     int32_t h = 0, e = 0;
-    int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim, j->starts ? j->starts[i] : 0,
+    const uint64_t zero = 0;
+    int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim,
+                         j->starts ? j->starts + (size_t)i * (size_t)j->ns : &zero, j->starts ? j->ns : 1,
                          j->pq, j->mode, j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL, NULL);
     if (j->hops) j->hops[i] = h;
     if (j->evals) j->evals[i] = e;
@@ -700,10 +711,10 @@ static int run_pool(void *(*fn)(void *), job_t *j, int nthreads) {
 int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq, int mode,
                       int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                       int32_t *popped, int nthreads) {
-  return orc_kernel_search_from(ix, queries, nq, NULL, pq, mode, use_fma, out, hops, evals, popped, nthreads);
+  return orc_kernel_search_from(ix, queries, nq, NULL, 1, pq, mode, use_fma, out, hops, evals, popped, nthreads);
 }
 
-int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, const uint64_t *starts,
+int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, const uint64_t *starts, int ns,
                            int pq, int mode, int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                            int32_t *popped, int nthreads) {
   if (check_index(ix) || !queries || !out || nq < 0 || pq < 2 || pq > 4095) return -1;
@@ -721,9 +732,12 @@ int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, co
   j.evals = evals;
   j.popped = popped;
   j.starts = starts;
-  if (starts)
-    for (int i = 0; i < nq; ++i)
+  j.ns = ns;
+  if (starts) {
+    if (ns < 1 || ns > pq) return -1;
+    for (size_t i = 0; i < (size_t)nq * (size_t)ns; ++i)
       if (starts[i] >= ix->n) return -1;
+  }
   return run_pool(kworker, &j, nthreads);
 }
 
@@ -736,7 +750,8 @@ int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int m
     return -1;
   }
   evlog L = {log, cap, 0};
-  ksearch_one(ix, query, 0, pq, mode, use_fma, &s, out, NULL, NULL, &L, NULL);
+  const uint64_t zero = 0;
+  ksearch_one(ix, query, &zero, 1, pq, mode, use_fma, &s, out, NULL, NULL, &L, NULL);
   if (n_events) *n_events = L.n;
   kscratch_free(&s);
   return 0;
@@ -754,7 +769,8 @@ int orc_kernel_search_trace(const orc_index *ix, const float *query, int pq, int
     return -1;
   }
   ktrace tr = {k, trace_hops, trace, 0, 0};
-  ksearch_one(ix, query, 0, pq, mode, use_fma, &s, out, hops, evals, NULL, &tr);
+  const uint64_t zero = 0;
+  ksearch_one(ix, query, &zero, 1, pq, mode, use_fma, &s, out, hops, evals, NULL, &tr);
   if (final_version) *final_version = tr.version;
   if (traced) *traced = tr.traced;
   kscratch_free(&s);
@@ -936,22 +952,32 @@ int orc_cpu_search(const orc_index *ix, const float *queries, int nq, int k, uin
 }
 
 int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
-                      int use_fma, uint64_t *starts) {
-  if (check_index(ix) || !queries || !entries || !starts || ne < 1) return -1;
+                      int ns, int use_fma, uint64_t *starts) {
+  if (check_index(ix) || !queries || !entries || !starts || ne < 1 || ns < 1 || ns > ne) return -1;
   for (int e = 0; e < ne; ++e)
     if (entries[e] >= ix->n) return -1;
+  float *bd = (float *)malloc(sizeof(float) * (size_t)ns);
+  if (!bd) return -1;
   for (int i = 0; i < nq; ++i) {
     const float *q = queries + (size_t)i * (size_t)ix->dim;
-    float best = 0.0f;
-    uint64_t bid = 0;
+    uint64_t *bi = starts + (size_t)i * (size_t)ns;
+    int have = 0; /* ascending (distance, id) list of the best `have` */
     for (int e = 0; e < ne; ++e) {
-      float d = orc_kernel_distance(ix->metric, ix->dim, q, row(ix, entries[e]), use_fma);
-      if (e == 0 || d < best || (d == best && entries[e] < bid)) {
-        best = d;
-        bid = entries[e];
+      const float d = orc_kernel_distance(ix->metric, ix->dim, q, row(ix, entries[e]), use_fma);
+      const uint64_t id = entries[e];
+      int pos = have;
+      while (pos > 0 && (d < bd[pos - 1] || (d == bd[pos - 1] && id < bi[pos - 1]))) --pos;
+      if (pos >= ns) continue;
+      int last = have < ns ? have : ns - 1;
+      for (int m = last; m > pos; --m) {
+        bd[m] = bd[m - 1];
+        bi[m] = bi[m - 1];
       }
+      bd[pos] = d;
+      bi[pos] = id;
+      if (have < ns) ++have;
     }
-    starts[i] = bid;
   }
+  free(bd);
   return 0;
 }

@@ -97,16 +97,17 @@ int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq,
                       int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                       int32_t *popped, int nthreads);
 
-/* orc_kernel_search with query i starting at vertex starts[i] instead of
- * vertex 0 (starts NULL: vertex 0 for all). */
-int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, const uint64_t *starts,
+/* orc_kernel_search with query i starting from the ns vertices
+ * starts[i*ns .. i*ns+ns-1] (queued and marked visited in that order before
+ * the first pop) instead of vertex 0 (starts NULL: vertex 0 for all). */
+int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, const uint64_t *starts, int ns,
                            int pq, int mode, int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                            int32_t *popped, int nthreads);
 
-/* Entry-point choice: starts[i] = the entry whose kernel distance to query i
- * is smallest (ties: the smaller id). */
+/* Entry-point choice: starts[i*ns ..] = the ns entries with the smallest
+ * kernel distance to query i, ascending by (distance, id). */
 int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
-                      int use_fma, uint64_t *starts);
+                      int ns, int use_fma, uint64_t *starts);
 
 /* One query with its decision log (at most cap events; *n_events gets the
  * number produced, which may exceed cap). */

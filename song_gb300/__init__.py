@@ -23,6 +23,7 @@ from .build import LIB_PATH
 
 SONG_OK, SONG_ERR_ARG, SONG_ERR_OOM, SONG_ERR_TIMEOUT, SONG_ERR_CUDA, SONG_ERR_IO = range(6)
 SONG_MAX_ENTRIES = 65536  # include/song_gb300.h
+SONG_MAX_STARTS = 8
 METRICS = {"l2": 0, "ip": 1, "cos": 2}
 STORAGES = {"f32": 0, "bf16": 1, "fp8": 2}
 MAX_PQ = 1023
@@ -87,7 +88,7 @@ def load_library():
     L.song_graph_build.restype = i32
     L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
     L.song_index_set_entries.restype = i32
-    L.song_index_set_entries.argtypes = [P, P, i32]
+    L.song_index_set_entries.argtypes = [P, P, i32, i32]
     L.song_graph_build_gpu.restype = i32
     L.song_graph_build_gpu.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, i32, P]
     L.song_index_set_rerank.restype = i32
@@ -215,12 +216,12 @@ class Index:
             raise ValueError("expected %d weights" % MLP_PARAMS)
         _check(load_library().song_index_set_early_exit(self._h, _ptr(w), float(threshold), int(min_hops), int(every)))
 
-    def set_entries(self, ids):
-        """Entry points: each query starts at the nearest of these vertices
-        (None or empty: vertex 0, the reference's start)."""
+    def set_entries(self, ids, starts=1):
+        """Entry points: each query starts from the `starts` nearest of these
+        vertices (None or empty: vertex 0, the reference's start)."""
         e = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint64)
         _check(load_library().song_index_set_entries(self._h, _ptr(e) if e is not None and e.size else None,
-                                                     0 if e is None else int(e.size)))
+                                                     0 if e is None else int(e.size), int(starts)))
 
     def set_hop_limit(self, max_hops):
         """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""

@@ -26,15 +26,21 @@
 namespace song {
 namespace {
 
+__device__ __forceinline__ bool closer(float d, uint32_t id, float bd, uint32_t bid) {
+  return d < bd || (d == bd && id < bid);
+}
+
 // One warp serves QB queries; lane e takes entries e, e+32, ... and reads
 // each entry row once, in 16-byte pieces, for all QB queries.  Rows and the
 // staged queries are zero-padded to dpad (a multiple of 4) floats: a padded
 // element adds fma(0, 0, t) = t, leaving every partial sum exactly as the
-// search leaves it.
-template <int METRIC, int QB>
+// search leaves it.  Each lane keeps its NS nearest entries per query in a
+// sorted register list; the warp then merges the lists, ns rounds of an xor
+// argmin, into starts[q*ns ..], ascending by (distance, id).
+template <int METRIC, int QB, int NS>
 __global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries, int nq, int dim, int dpad,
                                                             const float *entry_rows, const uint32_t *entry_ids,
-                                                            int n_entries, uint32_t *starts) {
+                                                            int n_entries, int ns, uint32_t *starts) {
   extern __shared__ float4 qs4[];  // (blockDim / 32) * QB query rows of dpad floats
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int q0 = (blockIdx.x * (blockDim.x >> 5) + wib) * QB;
@@ -46,13 +52,15 @@ __global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries
       qw[b * dpad + j] = (q0 + b < nq && j < dim) ? queries[static_cast<size_t>(q0 + b) * dim + j] : 0.0f;
   __syncwarp();
   const float4 *q4 = reinterpret_cast<const float4 *>(qw);
-  float best[QB];
-  uint32_t best_id[QB];
+  float bd[QB][NS];
+  uint32_t bi[QB][NS];
 #pragma unroll
-  for (int b = 0; b < QB; ++b) {
-    best[b] = 0.0f;
-    best_id[b] = 0xffffffffu;
-  }
+  for (int b = 0; b < QB; ++b)
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      bd[b][m] = __int_as_float(0x7f800000);  // +inf
+      bi[b][m] = 0xffffffffu;
+    }
   for (int e = lane; e < n_entries; e += 32) {
     const float4 *x4 = reinterpret_cast<const float4 *>(entry_rows + static_cast<size_t>(e) * dpad);
     float t[QB][32], l[32];
@@ -112,23 +120,46 @@ __global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries
       } else {
         d = 0.0f;
       }
-      if (best_id[b] == 0xffffffffu || d < best[b] || (d == best[b] && id < best_id[b])) {
-        best[b] = d;
-        best_id[b] = id;
+      // sorted insertion, the last entry falls off (positions read before written)
+#pragma unroll
+      for (int m = NS - 1; m >= 0; --m) {
+        const bool above = m > 0 && closer(d, id, bd[b][m > 0 ? m - 1 : 0], bi[b][m > 0 ? m - 1 : 0]);
+        const bool here = closer(d, id, bd[b][m], bi[b][m]);
+        if (above) {
+          bd[b][m] = bd[b][m - (m > 0 ? 1 : 0)];
+          bi[b][m] = bi[b][m - (m > 0 ? 1 : 0)];
+        } else if (here) {
+          bd[b][m] = d;
+          bi[b][m] = id;
+        }
       }
     }
   }
 #pragma unroll
   for (int b = 0; b < QB; ++b) {
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ob = __shfl_xor_sync(0xffffffffu, best[b], o);
-      const uint32_t oid = __shfl_xor_sync(0xffffffffu, best_id[b], o);
-      if (oid != 0xffffffffu && (best_id[b] == 0xffffffffu || ob < best[b] || (ob == best[b] && oid < best_id[b]))) {
-        best[b] = ob;
-        best_id[b] = oid;
+    int h = 0;  // this lane's next unused list position
+    for (int r = 0; r < ns; ++r) {
+      float d = __int_as_float(0x7f800000);
+      uint32_t id = 0xffffffffu;
+#pragma unroll
+      for (int m = 0; m < NS; ++m)
+        if (m == h) {
+          d = bd[b][m];
+          id = bi[b][m];
+        }
+      float wd = d;
+      uint32_t wid = id;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float od = __shfl_xor_sync(0xffffffffu, wd, o);
+        const uint32_t oid = __shfl_xor_sync(0xffffffffu, wid, o);
+        if (closer(od, oid, wd, wid)) {
+          wd = od;
+          wid = oid;
+        }
       }
+      if (id == wid && id != 0xffffffffu) ++h;  // entry ids are distinct: one lane owns the winner
+      if (lane == 0 && q0 + b < nq) starts[static_cast<size_t>(q0 + b) * ns + r] = wid;
     }
-    if (lane == 0 && q0 + b < nq) starts[q0 + b] = best_id[b];
   }
 }
 
@@ -147,54 +178,60 @@ __global__ void gather_entry_rows_kernel(const float *rows, uint32_t row_floats,
 
 int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s) {
   c.starts = nullptr;
+  c.n_starts = 1;
   if (ix->n_entries <= 0 || c.nq <= 0) return SONG_OK;
-  if (static_cast<size_t>(c.nq) > ix->cap_starts) {
+  if (ix->n_starts > c.pq) return fail(SONG_ERR_ARG, "%d start vertices need pq >= %d", ix->n_starts, ix->n_starts);
+  const size_t need = static_cast<size_t>(c.nq) * ix->n_starts;
+  if (need > ix->cap_starts) {
     if (ix->d_starts) cudaFree(ix->d_starts);
     ix->d_starts = nullptr;
     ix->cap_starts = 0;
-    cudaError_t e = cudaMalloc(&ix->d_starts, sizeof(uint32_t) * c.nq);
+    cudaError_t e = cudaMalloc(&ix->d_starts, sizeof(uint32_t) * need);
     if (e != cudaSuccess) return fail(SONG_ERR_OOM, "entry starts: %s", cudaGetErrorString(e));
-    ix->cap_starts = static_cast<size_t>(c.nq);
+    ix->cap_starts = need;
   }
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
   // warps per block: up to 8, within the default 48 KB of shared memory
-  const int per_warp = static_cast<int>(sizeof(float)) * dpad * (ix->dx.metric == SONG_METRIC_COS ? 1 : 2);
+  const int qb = ix->dx.metric == SONG_METRIC_COS ? 1 : 2;
+  const int per_warp = static_cast<int>(sizeof(float)) * dpad * qb;
   const int wpb = std::max(1, std::min(8, (48 * 1024) / per_warp));
-  switch (ix->dx.metric) {
-    case SONG_METRIC_L2:
-    case SONG_METRIC_IP: {
-      constexpr int QB = 2;
-      const size_t smem = sizeof(float) * dpad * wpb * QB;
-      const unsigned grid = static_cast<unsigned>((c.nq + wpb * QB - 1) / (wpb * QB));
-      if (ix->dx.metric == SONG_METRIC_L2)
-        nearest_entry_kernel<SONG_METRIC_L2, QB><<<grid, 32 * wpb, smem, s>>>(
-            c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ix->d_starts);
-      else
-        nearest_entry_kernel<SONG_METRIC_IP, QB><<<grid, 32 * wpb, smem, s>>>(
-            c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ix->d_starts);
-      break;
-    }
-    default: {
-      const size_t smem = sizeof(float) * dpad * wpb;
-      const unsigned grid = static_cast<unsigned>((c.nq + wpb - 1) / wpb);
-      nearest_entry_kernel<SONG_METRIC_COS, 1><<<grid, 32 * wpb, smem, s>>>(
-          c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ix->d_starts);
-      break;
-    }
+  const size_t smem = static_cast<size_t>(per_warp) * wpb;
+  const unsigned grid = static_cast<unsigned>((c.nq + wpb * qb - 1) / (wpb * qb));
+  const int ns = ix->n_starts;
+  const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
+#define SONG_ENTRY_LAUNCH(M, QB, NS)                                                                    \
+  nearest_entry_kernel<M, QB, NS><<<grid, 32 * wpb, smem, s>>>(c.queries, c.nq, dim, dpad, ix->d_entry_rows, \
+                                                               ix->d_entry_ids, ix->n_entries, ns, ix->d_starts)
+#define SONG_ENTRY_BY_NS(M, QB)              \
+  switch (NSel) {                            \
+    case 1: SONG_ENTRY_LAUNCH(M, QB, 1); break; \
+    case 2: SONG_ENTRY_LAUNCH(M, QB, 2); break; \
+    case 4: SONG_ENTRY_LAUNCH(M, QB, 4); break; \
+    default: SONG_ENTRY_LAUNCH(M, QB, 8); break; \
   }
+  switch (ix->dx.metric) {
+    case SONG_METRIC_L2: SONG_ENTRY_BY_NS(SONG_METRIC_L2, 2); break;
+    case SONG_METRIC_IP: SONG_ENTRY_BY_NS(SONG_METRIC_IP, 2); break;
+    default: SONG_ENTRY_BY_NS(SONG_METRIC_COS, 1); break;
+  }
+#undef SONG_ENTRY_BY_NS
+#undef SONG_ENTRY_LAUNCH
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "entry launch: %s", cudaGetErrorString(e));
   c.starts = ix->d_starts;
+  c.n_starts = ix->n_starts;
   return SONG_OK;
 }
 
 }  // namespace song
 
-extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int count) {
+extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int count, int starts) {
   using namespace song;
   clear_error();
   if (!ix) return fail(SONG_ERR_ARG, "null index");
   if (count < 0 || count > SONG_MAX_ENTRIES) return fail(SONG_ERR_ARG, "entry count must be 0..%d", SONG_MAX_ENTRIES);
+  if (count > 0 && (starts < 1 || starts > SONG_MAX_STARTS || starts > count))
+    return fail(SONG_ERR_ARG, "starts must be 1..min(%d, entry count)", SONG_MAX_STARTS);
   if (count > 0 && !ids) return fail(SONG_ERR_ARG, "null entry ids");
   std::vector<uint32_t> h(static_cast<size_t>(count));
   for (int i = 0; i < count; ++i) {
@@ -228,5 +265,6 @@ extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int c
     return fail(e == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "entries: %s", cudaGetErrorString(e));
   }
   ix->n_entries = count;
+  ix->n_starts = starts;
   return SONG_OK;
 }

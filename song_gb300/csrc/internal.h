@@ -42,7 +42,8 @@ struct SearchCall {
   float *trace = nullptr;          // per-hop features, nq x trace_hops x 6, or null
   int trace_hops = 0;
   int32_t *trace_final = nullptr;  // nq x 2: final top-k version, hops traced
-  const uint32_t *starts = nullptr;  // per-query start vertex (entry points), null = vertex 0
+  const uint32_t *starts = nullptr;  // nq x n_starts start vertices (entry points), null = vertex 0
+  int n_starts = 1;
 };
 
 // Launch the plain search.  Returns a cudaError_t-compatible code (0 ok) or
@@ -95,6 +96,7 @@ struct song_index {
   uint32_t *d_entry_ids = nullptr;
   float *d_entry_rows = nullptr;
   int n_entries = 0;
+  int n_starts = 1;  // start vertices per query (nearest entries)
   uint32_t *d_starts = nullptr;
   size_t cap_starts = 0;
   uint64_t device_bytes = 0;

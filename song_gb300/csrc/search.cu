@@ -164,6 +164,7 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
   p.trace_hops = c.trace_hops;
   p.trace_final = c.trace_final;
   p.starts = c.starts;
+  p.n_starts = c.starts ? c.n_starts : 1;
   if (learned) {
     if (ix.storage == 2) return -1;
     return launch_learned(p, ix.storage, ix.metric, L.H, L.S, stream);

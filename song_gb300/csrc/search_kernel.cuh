@@ -83,7 +83,8 @@ struct Params {
   float *trace;           // [nq][trace_hops][TRACE_FIELDS] or null
   int trace_hops;
   int32_t *trace_final;   // [nq]: final top-k version, hops traced
-  const uint32_t *starts; // [nq] start vertex of each query, or null: vertex 0
+  const uint32_t *starts; // [nq][n_starts] start vertices of each query, or null: vertex 0
+  int n_starts;
 };
 
 template <int METRIC>
@@ -295,22 +296,25 @@ struct QueryStats {
 // (LEARNED) receives the per-hop features or is null.  False if a bulk copy
 // never completed.
 template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
-__device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const float *qsrc, uint32_t start, int pq,
-                                          int k, uint64_t *o, float *trace, QueryStats &st, int lane) {
+__device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const float *qsrc, const uint32_t *starts,
+                                          int ns, int pq, int k, uint64_t *o, float *trace, QueryStats &st,
+                                          int lane) {
   typename VisitedOf<LEARNED>::type vh = VisitedOf<LEARNED>::make(w.tab, pq);
   RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
   constexpr int C = RegQueue<S>::C;
   const int nslots = 1 << p.shift;
   for (int j = lane; j < p.dim; j += 32) w.qv[j] = qsrc[j];
   vh.clear(lane);
-  // Adjacency row of the start vertex (vertex 0 unless entry points are
-  // set), the first vertex popped.
-  uint32_t next_id = start;
-  uint32_t a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(start) << p.shift) + lane) : 0u;
+  // Start vertices: vertex 0 (the reference's), or the ns entry points the
+  // pre-pass chose (lane i holds start i).  Prefetch the first start's row.
+  if (!starts) ns = 1;
+  const uint32_t sid = (starts && lane < ns) ? starts[lane] : 0u;
+  uint32_t next_id = __shfl_sync(FULL, sid, 0);
+  uint32_t a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
 
-  // warp_astar_accelerator.h:115-176: distance to the start, queue = {start}.
+  // warp_astar_accelerator.h:115-176: distances to the starts, queue = {starts}.
   float cd;
-  if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, 1, start, cd, lane)) {
+  if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, ns, sid, cd, lane)) {
     return false;
   }
   const float d0 = __shfl_sync(FULL, cd, 0);
@@ -326,10 +330,20 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
   // infinite ones; a pop shifts the window one place left.
 #pragma unroll
   for (int j = 0; j < S; ++j) Q.v[j] = (lane * S + j) >= C - pq ? ~0ull : 0ull;
-  Q.insert_evict(make_key(d0, start), lane);
-  qn = 1;
-  vh.add(start, lane);
-  int hops = 0, evals = 1;
+  for (int i = 0; i < ns; ++i) {  // in start order, as the oracle queues them
+    const uint32_t id = __shfl_sync(FULL, sid, i);
+    Q.insert_evict(make_key(__shfl_sync(FULL, cd, i), id), lane);
+    vh.add(id, lane);
+  }
+  qn = ns;
+  if (ns > 1) {  // the first pop is the nearest start: prefetch its row instead
+    const uint32_t mid = key_id(warp_min_u64(lane < ns ? make_key(cd, sid) : ~0ull));
+    if (mid != next_id) {
+      next_id = mid;
+      a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(mid) << p.shift) + lane) : 0u;
+    }
+  }
+  int hops = 0, evals = ns;
   int version = 0;           // number of changes of the top-k set (LEARNED)
   int last_change = 0;       // hop of the latest change (LEARNED)
   uint64_t kth_key = ~0ull;  // k-th smallest key of T, ~0 while tn < k (LEARNED)
@@ -514,7 +528,9 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
     if (LEARNED && p.trace) trace = p.trace + static_cast<size_t>(qid) * p.trace_hops * TRACE_FIELDS;
     QueryStats st;
     if (!run_query<METRIC, STORAGE, H, S, LEARNED>(p, w, p.queries + static_cast<size_t>(qid) * p.dim,
-                                                   p.starts ? p.starts[qid] : 0u, p.pq,
+                                                   p.starts ? p.starts + static_cast<size_t>(qid) * p.n_starts
+                                                            : nullptr,
+                                                   p.n_starts, p.pq,
                                                    p.k, p.out + static_cast<size_t>(qid) * p.k, trace, st,
                                                    lane)) {
       if (lane == 0) atomicOr(p.error, 1);

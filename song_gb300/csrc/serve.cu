@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1)
     (void)ld_acquire_sys(&ctl->published);  // every lane: order the entry's and query's reads
     const ServeEntry e = ring[idx & ring_mask];
     QueryStats st;
-    if (!run_query<METRIC, STORAGE, H, S, false>(p, w, reinterpret_cast<const float *>(e.query), 0u, e.pq, e.k,
+    if (!run_query<METRIC, STORAGE, H, S, false>(p, w, reinterpret_cast<const float *>(e.query), nullptr, 1, e.pq, e.k,
                                                  reinterpret_cast<uint64_t *>(e.out), nullptr, st, lane)) {
       if (lane == 0) atomicOr(p.error, 1);
       return;

@@ -1,8 +1,9 @@
-"""Entry points (song_index_set_entries): every query starts at its nearest
-entry vertex instead of vertex 0.  The entry choice and the search from it
-must equal the oracle's (orc_nearest_entry + orc_kernel_search_from) bit for
-bit, for F32 and BF16 storage and for the learned kernel with its exit off;
-clearing the entries restores the reference's start at vertex 0."""
+"""Entry points (song_index_set_entries): every query starts from its
+nearest entry vertices (one or several) instead of vertex 0.  The entry
+choice and the search from it must equal the oracle's (orc_nearest_entry +
+orc_kernel_search_from) bit for bit, for F32 and BF16 storage and for the
+learned kernel with its exit off; clearing the entries restores the
+reference's start at vertex 0."""
 import numpy as np
 import pytest
 
@@ -16,16 +17,17 @@ def _entries(n, count, seed):
     return np.sort(rng.choice(n, count, replace=False)).astype(np.uint64)
 
 
+@pytest.mark.parametrize("ns", [1, 3, 8])
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_search_from_nearest_entry_matches_oracle(song, oracle, name):
+def test_search_from_nearest_entries_matches_oracle(song, oracle, name, ns):
     g = load_golden(name)
     shift, metric = int(g["shift"]), int(g["metric"])
     ox = oracle.OracleIndex(g["data"], g["graph"], shift, metric)
     ent = _entries(g["data"].shape[0], 64, 5)
-    starts = ox.nearest_entry(g["queries"], ent)
-    assert len(set(starts.tolist())) > 1  # the queries do not all start at one vertex
+    starts = ox.nearest_entry(g["queries"], ent, ns=ns)
+    assert len(set(np.asarray(starts).reshape(len(starts), -1)[:, 0].tolist())) > 1
     with song.Index(g["graph"], g["data"], shift, metric) as ix:
-        ix.set_entries(ent)
+        ix.set_entries(ent, starts=ns)
         for pq in (10, 50, 100):
             ids, hops, evals = ix.search(g["queries"], pq, pq, stats=True)
             o_ids, o_hops, o_evals, _ = ox.kernel_search_from(g["queries"], starts, pq, oracle.MODE_LEX)
@@ -42,10 +44,10 @@ def test_entries_with_low_precision_rows(song, oracle, storage):
     g = load_golden("cos_s5_d26")
     shift, metric = int(g["shift"]), int(g["metric"])
     ent = _entries(g["data"].shape[0], 100, 6)
-    starts = oracle.OracleIndex(g["data"], g["graph"], shift, metric).nearest_entry(g["queries"], ent)
+    starts = oracle.OracleIndex(g["data"], g["graph"], shift, metric).nearest_entry(g["queries"], ent, ns=4)
     with song.Index(g["graph"], g["data"], shift, metric, storage=storage) as ix:
         ix.set_rerank(0)
-        ix.set_entries(ent)
+        ix.set_entries(ent, starts=4)
         deq = song.dequantize_rows(ix.rows(), storage, g["data"].shape[1])
         ox = oracle.OracleIndex(deq, g["graph"], shift, metric)
         ids, hops, evals = ix.search(g["queries"], 60, 60, stats=True)
@@ -60,9 +62,9 @@ def test_learned_kernel_from_entries_matches_exact_visited_oracle(song, oracle):
     shift, metric = int(g["shift"]), int(g["metric"])
     ox = oracle.OracleIndex(g["data"], g["graph"], shift, metric)
     ent = _entries(g["data"].shape[0], 50, 7)
-    starts = ox.nearest_entry(g["queries"], ent)
+    starts = ox.nearest_entry(g["queries"], ent, ns=2)
     with song.Index(g["graph"], g["data"], shift, metric) as ix:
-        ix.set_entries(ent)
+        ix.set_entries(ent, starts=2)
         dq = torch.from_numpy(g["queries"]).cuda()
         ids, hops, evals = LE.evaluate(ix, dq, 100, 100, max_hops=1 << 30)
     o_ids, o_hops, o_evals, _ = ox.kernel_search_from(g["queries"], starts, 100, oracle.MODE_LEX_EXACT)
@@ -77,5 +79,12 @@ def test_entry_arguments_are_checked(song):
             ix.set_entries(np.array([0, n], dtype=np.uint64))
         with pytest.raises(song.SongError):
             ix.set_entries(np.zeros(song.SONG_MAX_ENTRIES + 1, dtype=np.uint64))
+        with pytest.raises(song.SongError):  # more starts than entries
+            ix.set_entries(np.array([1, 2], dtype=np.uint64), starts=3)
+        with pytest.raises(song.SongError):
+            ix.set_entries(np.arange(20, dtype=np.uint64), starts=song.SONG_MAX_STARTS + 1)
+        ix.set_entries(np.arange(20, dtype=np.uint64), starts=8)
+        with pytest.raises(song.SongError):  # starts > pq
+            ix.search(g["queries"][:3], 5, 5)
         ix.set_entries(np.array([n - 1], dtype=np.uint64))  # a single entry is allowed
         assert ix.search(g["queries"][:3], 20, 5).shape == (3, 5)
