@@ -35,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PQ_SWEEP = [50, 100, 150, 200, 250, 300, 350, 400, 500, 600, 800, 1000]
+PQ_SWEEP = [50, 75, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800, 1000]
 CPU_K_SWEEP = [10, 20, 40, 80, 150, 300, 500, 800, 1200, 1600, 2000]
 
 
@@ -68,7 +68,7 @@ def parse_args():
                         "learned / plain / entries: that path only; "
                         "precision: storage error and recall table; serve: Poisson request stream; "
                         "build: graph construction, GPU searches vs the CPU builder")
-    p.add_argument("--entries", type=int, default=4096, help="entry vertices of the entries arm (sampled, seeded)")
+    p.add_argument("--entries", type=int, default=8192, help="entry vertices of the entries arm (sampled, seeded)")
     p.add_argument("--starts", type=int, default=4, help="start vertices per query: its nearest entries")
     p.add_argument("--serve-rate", type=float, default=20000.0, help="mean offered queries/s (serve)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="length of each request stream (serve)")
