@@ -174,6 +174,21 @@ int song_index_set_hop_limit(song_index *index, int max_hops);
 #define SONG_MAX_STARTS 8
 int song_index_set_entries(song_index *index, const uint64_t *ids, int count, int starts);
 
+/* Two-level entry points, for large entry sets (no counterpart in the
+ * reference).  ids[0..coarse-1] are coarse entries, each its own cluster;
+ * every other entry joins the cluster of its nearest coarse entry (its FP32
+ * row as the query, ties to the smaller id), computed here on the GPU.  Each
+ * query then probes its `probes` nearest coarse entries and starts from the
+ * `starts` nearest entries of those clusters (starts <= probes <= min(
+ * SONG_MAX_STARTS, coarse)): one pass over the coarse rows and the probed
+ * clusters instead of all entries.  Distinct ids; rows of up to 640 floats.
+ * Replaces any entries set before; song_index_set_entries(ix, NULL, 0, 1)
+ * clears them. */
+#define SONG_MAX_ENTRIES_2LEVEL (1 << 20)
+#define SONG_MAX_COARSE 16384
+int song_index_set_entries_2level(song_index *index, const uint64_t *ids, int count, int coarse, int probes,
+                                  int starts);
+
 /* Training of the early-exit network (no counterpart in the reference), all
  * buffers on the device, ordered on `stream`: x n x 5 features, y n labels
  * (0/1), w n sample weights or NULL, perm epochs x n sample indices or NULL

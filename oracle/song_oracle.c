@@ -981,3 +981,60 @@ int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const u
   free(bd);
   return 0;
 }
+
+/* Two-level entry choice.  Entries ids[0..coarse-1] are the coarse entries;
+ * each forms its own cluster, and every other entry joins the cluster of its
+ * nearest coarse entry (kernel distance, the entry's FP32 row as the query,
+ * ties to the smaller id).  A query probes its `probes` nearest coarse
+ * entries and starts from the `ns` nearest entries of those clusters
+ * (ascending by (distance, id); ns <= probes). */
+int orc_nearest_entry_2level(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
+                             int coarse, int probes, int ns, int use_fma, uint64_t *starts) {
+  if (check_index(ix) || !queries || !entries || !starts || ne < 1 || coarse < 1 || coarse > ne || probes < 1 ||
+      probes > coarse || ns < 1 || ns > probes)
+    return -1;
+  for (int e = 0; e < ne; ++e)
+    if (entries[e] >= ix->n) return -1;
+  int *cl = (int *)malloc(sizeof(int) * (size_t)ne);
+  uint64_t *pc = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)probes);
+  uint64_t *cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)ne);
+  if (!cl || !pc || !cand) {
+    free(cl);
+    free(pc);
+    free(cand);
+    return -1;
+  }
+  for (int f = 0; f < ne; ++f) {
+    if (f < coarse) {
+      cl[f] = f;
+      continue;
+    }
+    uint64_t best;
+    if (orc_nearest_entry(ix, row(ix, entries[f]), 1, entries, coarse, 1, use_fma, &best) != 0) {
+      free(cl);
+      free(pc);
+      free(cand);
+      return -1;
+    }
+    int c = 0;
+    while (entries[c] != best) ++c; /* the coarse position of that id */
+    cl[f] = c;
+  }
+  int rc = 0;
+  for (int i = 0; i < nq && rc == 0; ++i) {
+    const float *q = queries + (size_t)i * (size_t)ix->dim;
+    rc = orc_nearest_entry(ix, q, 1, entries, coarse, probes, use_fma, pc);
+    int nc = 0;
+    for (int f = 0; f < ne && rc == 0; ++f)
+      for (int p = 0; p < probes; ++p)
+        if (entries[cl[f]] == pc[p]) {
+          cand[nc++] = entries[f];
+          break;
+        }
+    if (rc == 0) rc = orc_nearest_entry(ix, q, 1, cand, nc, ns, use_fma, starts + (size_t)i * (size_t)ns);
+  }
+  free(cl);
+  free(pc);
+  free(cand);
+  return rc;
+}

@@ -109,6 +109,14 @@ int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, co
 int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
                       int ns, int use_fma, uint64_t *starts);
 
+/* Two-level entry choice: entries[0..coarse-1] are coarse entries, each its
+ * own cluster; every other entry joins its nearest coarse entry's cluster
+ * (the entry's row as the query, ties to the smaller id).  Query i probes its
+ * `probes` nearest coarse entries and gets the ns nearest entries of those
+ * clusters in starts[i*ns ..] (ascending; ns <= probes <= coarse). */
+int orc_nearest_entry_2level(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
+                             int coarse, int probes, int ns, int use_fma, uint64_t *starts);
+
 /* One query with its decision log (at most cap events; *n_events gets the
  * number produced, which may exceed cap). */
 int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int mode, int use_fma,

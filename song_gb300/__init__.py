@@ -33,7 +33,7 @@ NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 EXPORTED = [
     "song_status_string", "song_last_error", "song_index_create", "song_index_load",
     "song_index_free", "song_index_info", "song_search", "song_search_device",
-    "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_index_set_entries", "song_debug_fixhash", "song_search_noalloc",
+    "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_index_set_entries", "song_index_set_entries_2level", "song_debug_fixhash", "song_search_noalloc",
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
     "song_index_set_hop_limit", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
@@ -89,6 +89,8 @@ def load_library():
     L.song_graph_build.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, P]
     L.song_index_set_entries.restype = i32
     L.song_index_set_entries.argtypes = [P, P, i32, i32]
+    L.song_index_set_entries_2level.restype = i32
+    L.song_index_set_entries_2level.argtypes = [P, P, i32, i32, i32, i32]
     L.song_graph_build_gpu.restype = i32
     L.song_graph_build_gpu.argtypes = [P, u64, i32, i32, i32, i32, i32, i32, i32, i32, i32, P]
     L.song_index_set_rerank.restype = i32
@@ -216,12 +218,19 @@ class Index:
             raise ValueError("expected %d weights" % MLP_PARAMS)
         _check(load_library().song_index_set_early_exit(self._h, _ptr(w), float(threshold), int(min_hops), int(every)))
 
-    def set_entries(self, ids, starts=1):
+    def set_entries(self, ids, starts=1, coarse=0, probes=0):
         """Entry points: each query starts from the `starts` nearest of these
-        vertices (None or empty: vertex 0, the reference's start)."""
+        vertices (None or empty: vertex 0, the reference's start).  coarse >
+        0: two-level choice, ids[:coarse] are the coarse entries and each
+        query searches only its `probes` nearest coarse entries' clusters."""
         e = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint64)
-        _check(load_library().song_index_set_entries(self._h, _ptr(e) if e is not None and e.size else None,
-                                                     0 if e is None else int(e.size), int(starts)))
+        L = load_library()
+        if coarse > 0:
+            _check(L.song_index_set_entries_2level(self._h, _ptr(e), int(e.size), int(coarse), int(probes),
+                                                   int(starts)))
+            return
+        _check(L.song_index_set_entries(self._h, _ptr(e) if e is not None and e.size else None,
+                                        0 if e is None else int(e.size), int(starts)))
 
     def set_hop_limit(self, max_hops):
         """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""

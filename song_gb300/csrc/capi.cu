@@ -101,6 +101,8 @@ void release(song_index *ix) {
   cudaFree(ix->d_stats);
   cudaFree(ix->d_entry_ids);
   cudaFree(ix->d_entry_rows);
+  cudaFree(ix->d_coarse_rows);
+  cudaFree(ix->d_offsets);
   cudaFree(ix->d_starts);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;

@@ -38,7 +38,8 @@ __device__ __forceinline__ bool closer(float d, uint32_t id, float bd, uint32_t 
 // sorted register list; the warp then merges the lists, ns rounds of an xor
 // argmin, into starts[q*ns ..], ascending by (distance, id).
 template <int METRIC, int QB, int NS>
-__global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries, int nq, int dim, int dpad,
+__global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries, int nq, int qstride, int dim,
+                                                            int dpad,
                                                             const float *entry_rows, const uint32_t *entry_ids,
                                                             int n_entries, int ns, uint32_t *starts) {
   extern __shared__ float4 qs4[];  // (blockDim / 32) * QB query rows of dpad floats
@@ -49,7 +50,7 @@ __global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries
   float *qw = reinterpret_cast<float *>(qs4) + static_cast<size_t>(wib) * QB * dpad;
   for (int b = 0; b < QB; ++b)
     for (int j = lane; j < dpad; j += 32)
-      qw[b * dpad + j] = (q0 + b < nq && j < dim) ? queries[static_cast<size_t>(q0 + b) * dim + j] : 0.0f;
+      qw[b * dpad + j] = (q0 + b < nq && j < dim) ? queries[static_cast<size_t>(q0 + b) * qstride + j] : 0.0f;
   __syncwarp();
   const float4 *q4 = reinterpret_cast<const float4 *>(qw);
   float bd[QB][NS];
@@ -171,7 +172,8 @@ __global__ void __launch_bounds__(256) nearest_entry_kernel(const float *queries
 // e of the tile.  Partial sums, order and merge are those of
 // nearest_entry_kernel.
 template <int METRIC, int QB, int NS>
-__global__ void __launch_bounds__(256) nearest_entry_tiled_kernel(const float *queries, int nq, int dim, int dpad,
+__global__ void __launch_bounds__(256) nearest_entry_tiled_kernel(const float *queries, int nq, int qstride, int dim,
+                                                            int dpad,
                                                                   const float *entry_rows,
                                                                   const uint32_t *entry_ids, int n_entries, int ns,
                                                                   uint32_t *starts) {
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(256) nearest_entry_tiled_kernel(const float *q
   float *qw = reinterpret_cast<float *>(sm4 + TILE * rs4) + static_cast<size_t>(wib) * QB * dpad;
   for (int b = 0; b < QB; ++b)
     for (int j = lane; j < dpad; j += 32)
-      qw[b * dpad + j] = (q0 + b < nq && j < dim) ? queries[static_cast<size_t>(q0 + b) * dim + j] : 0.0f;
+      qw[b * dpad + j] = (q0 + b < nq && j < dim) ? queries[static_cast<size_t>(q0 + b) * qstride + j] : 0.0f;
   const float4 *q4 = reinterpret_cast<const float4 *>(qw);
   float bd[QB][NS];
   uint32_t bi[QB][NS];
@@ -317,7 +319,265 @@ __global__ void gather_entry_rows_kernel(const float *rows, uint32_t row_floats,
   }
 }
 
+// The ns nearest of n entry rows (ids) for each of nq query rows (stride
+// qstride floats), into out[q*ns ..].
+cudaError_t launch_nearest(const float *queries, int nq, int qstride, int dim, int dpad, int metric,
+                           const float *rows, const uint32_t *ids, int n, int ns, uint32_t *out, cudaStream_t s) {
+  // warps per block: up to 8, within the default 48 KB of shared memory;
+  // rows of up to 1 KB are staged through shared memory in 32-row tiles
+  const int qb = metric == SONG_METRIC_COS ? 1 : 2;
+  const int per_warp = static_cast<int>(sizeof(float)) * dpad * qb;
+  const int tile_bytes = 32 * (dpad / 4 + 1) * 16;
+  const bool tiled = dpad * 4 <= 1024 && tile_bytes + per_warp <= 48 * 1024;
+  const int avail = 48 * 1024 - (tiled ? tile_bytes : 0);
+  const int wpb = std::max(1, std::min(8, avail / per_warp));
+  const size_t smem = static_cast<size_t>(per_warp) * wpb + (tiled ? tile_bytes : 0);
+  const unsigned grid = static_cast<unsigned>((nq + wpb * qb - 1) / (wpb * qb));
+  const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
+#define SONG_ENTRY_LAUNCH(M, QB, NS)                                                                        \
+  do {                                                                                                   \
+    if (tiled)                                                                                           \
+      nearest_entry_tiled_kernel<M, QB, NS><<<grid, 32 * wpb, smem, s>>>(queries, nq, qstride, dim, dpad,  \
+                                                                         rows, ids, n, ns, out);         \
+    else                                                                                                 \
+      nearest_entry_kernel<M, QB, NS><<<grid, 32 * wpb, smem, s>>>(queries, nq, qstride, dim, dpad, rows, \
+                                                                   ids, n, ns, out);                     \
+  } while (0)
+#define SONG_ENTRY_BY_NS(M, QB)                 \
+  switch (NSel) {                               \
+    case 1: SONG_ENTRY_LAUNCH(M, QB, 1); break; \
+    case 2: SONG_ENTRY_LAUNCH(M, QB, 2); break; \
+    case 4: SONG_ENTRY_LAUNCH(M, QB, 4); break; \
+    default: SONG_ENTRY_LAUNCH(M, QB, 8); break; \
+  }
+  switch (metric) {
+    case SONG_METRIC_L2: SONG_ENTRY_BY_NS(SONG_METRIC_L2, 2); break;
+    case SONG_METRIC_IP: SONG_ENTRY_BY_NS(SONG_METRIC_IP, 2); break;
+    default: SONG_ENTRY_BY_NS(SONG_METRIC_COS, 1); break;
+  }
+#undef SONG_ENTRY_BY_NS
+#undef SONG_ENTRY_LAUNCH
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Two-level choice: the probes nearest coarse entries, then the ns nearest
+// entries of their clusters.
+// ---------------------------------------------------------------------------
+
+// The search distance of one entry row (padded to d4 float4s) to one staged
+// query, computed by one thread exactly as nearest_entry_kernel does.
+template <int METRIC, bool GLOBAL>
+__device__ __forceinline__ float entry_distance(const float4 *x4, const float4 *q4, int d4) {
+  float t[32], l[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) t[i] = l[i] = 0.0f;
+  for (int c0 = 0; c0 < d4; c0 += 8) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (c0 + i < d4) {
+        const float4 xv = GLOBAL ? __ldg(x4 + c0 + i) : x4[c0 + i];
+        const float4 qv = q4[c0 + i];
+        const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+        const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (METRIC == SONG_METRIC_L2) {
+            const float d = __fsub_rn(qq[c], xs[c]);
+            t[4 * i + c] = __fmaf_rn(d, d, t[4 * i + c]);
+          } else {
+            t[4 * i + c] = __fmaf_rn(qq[c], xs[c], t[4 * i + c]);
+            if (METRIC == SONG_METRIC_COS) l[4 * i + c] = __fmaf_rn(xs[c], xs[c], l[4 * i + c]);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int i = 0; i < off; ++i) {
+      t[i] = __fadd_rn(t[i], t[i + off]);
+      if (METRIC == SONG_METRIC_COS) l[i] = __fadd_rn(l[i], l[i + off]);
+    }
+  }
+  if (METRIC == SONG_METRIC_L2) return t[0];
+  if (METRIC == SONG_METRIC_IP) return -t[0];
+  if (l[0] != 0.0f) {
+    const float sign = t[0] < 0.0f ? 1.0f : -1.0f;
+    return __fdiv_rn(__fmul_rn(__fmul_rn(sign, t[0]), t[0]), l[0]);
+  }
+  return 0.0f;
+}
+
+// Sorted insertion into a lane's NS best (distance, id); the last falls off.
+template <int NS>
+__device__ __forceinline__ void list_insert(float (&bd)[NS], uint32_t (&bi)[NS], float d, uint32_t id) {
+#pragma unroll
+  for (int m = NS - 1; m >= 0; --m) {
+    const bool above = m > 0 && closer(d, id, bd[m > 0 ? m - 1 : 0], bi[m > 0 ? m - 1 : 0]);
+    const bool here = closer(d, id, bd[m], bi[m]);
+    if (above) {
+      bd[m] = bd[m - (m > 0 ? 1 : 0)];
+      bi[m] = bi[m - (m > 0 ? 1 : 0)];
+    } else if (here) {
+      bd[m] = d;
+      bi[m] = id;
+    }
+  }
+}
+
+// One round of the warp merge: the nearest head over the lanes' lists (every
+// lane gets it); the owning lane moves past it.
+template <int NS>
+__device__ __forceinline__ uint32_t list_take(const float (&bd)[NS], const uint32_t (&bi)[NS], int &h) {
+  float d = __int_as_float(0x7f800000);
+  uint32_t id = 0xffffffffu;
+#pragma unroll
+  for (int m = 0; m < NS; ++m)
+    if (m == h) {
+      d = bd[m];
+      id = bi[m];
+    }
+  float wd = d;
+  uint32_t wid = id;
+  for (int o = 16; o > 0; o >>= 1) {
+    const float od = __shfl_xor_sync(0xffffffffu, wd, o);
+    const uint32_t oid = __shfl_xor_sync(0xffffffffu, wid, o);
+    if (closer(od, oid, wd, wid)) {
+      wd = od;
+      wid = oid;
+    }
+  }
+  if (id == wid && id != 0xffffffffu) ++h;
+  return wid;
+}
+
+// One warp per query.  Phase 1 streams the coarse rows (sorted by id, so the
+// position is the tie order) through shared-memory tiles shared by the
+// block; phase 2 reads the probed clusters' rows (cluster-ordered block in
+// L2), each lane a row.
+template <int METRIC, int NS, int NP>
+__global__ void __launch_bounds__(256) nearest_entry_2level_kernel(const float *queries, int nq, int dim, int dpad,
+                                                                   const float *coarse_rows, int n_coarse,
+                                                                   const float *fine_rows, const uint32_t *fine_ids,
+                                                                   const uint32_t *offsets, int probes, int ns,
+                                                                   uint32_t *starts) {
+  extern __shared__ float4 sm4[];
+  constexpr int TILE = 32;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int qi = blockIdx.x * nwarps + wib;
+  const bool active = qi < nq;
+  const int d4 = dpad >> 2, rs4 = d4 + 1;
+  float4 *tile = sm4;
+  float *qw = reinterpret_cast<float *>(sm4 + TILE * rs4) + static_cast<size_t>(wib) * (dpad + 32);
+  uint32_t *pw = reinterpret_cast<uint32_t *>(qw + dpad);  // this warp's probed clusters (<= 8)
+  for (int j = lane; j < dpad; j += 32) qw[j] = (active && j < dim) ? queries[static_cast<size_t>(qi) * dim + j] : 0.0f;
+  const float4 *q4 = reinterpret_cast<const float4 *>(qw);
+  float pd[NP];
+  uint32_t pi[NP];
+#pragma unroll
+  for (int m = 0; m < NP; ++m) {
+    pd[m] = __int_as_float(0x7f800000);
+    pi[m] = 0xffffffffu;
+  }
+  for (int t0 = 0; t0 < n_coarse; t0 += TILE) {
+    const int rows = min(TILE, n_coarse - t0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < rows * d4; i += blockDim.x) {
+      const int r = i / d4, c = i - r * d4;
+      tile[r * rs4 + c] = __ldg(reinterpret_cast<const float4 *>(coarse_rows + static_cast<size_t>(t0 + r) * dpad) + c);
+    }
+    __syncthreads();
+    if (active && lane < rows)
+      list_insert<NP>(pd, pi, entry_distance<METRIC, false>(tile + lane * rs4, q4, d4), static_cast<uint32_t>(t0 + lane));
+  }
+  if (!active) return;
+  int h = 0;
+  for (int r = 0; r < probes; ++r) {
+    const uint32_t c = list_take<NP>(pd, pi, h);
+    if (lane == 0) pw[r] = c;
+  }
+  __syncwarp();
+  float bd[NS];
+  uint32_t bi[NS];
+#pragma unroll
+  for (int m = 0; m < NS; ++m) {
+    bd[m] = __int_as_float(0x7f800000);
+    bi[m] = 0xffffffffu;
+  }
+  for (int r = 0; r < probes; ++r) {
+    const uint32_t c = pw[r];
+    const uint32_t end = offsets[c + 1];
+    for (uint32_t e = offsets[c] + lane; e < end; e += 32) {
+      const float d = entry_distance<METRIC, true>(reinterpret_cast<const float4 *>(fine_rows + static_cast<size_t>(e) * dpad),
+                                                   q4, d4);
+      list_insert<NS>(bd, bi, d, fine_ids[e]);
+    }
+  }
+  h = 0;
+  for (int r = 0; r < ns; ++r) {
+    const uint32_t id = list_take<NS>(bd, bi, h);
+    if (lane == 0) starts[static_cast<size_t>(qi) * ns + r] = id;
+  }
+}
+
+cudaError_t launch_2level(const song_index *ix, const float *queries, int nq, uint32_t *out, cudaStream_t s) {
+  const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
+  const int tile_bytes = 32 * (dpad / 4 + 1) * 16;
+  const int per_warp = (dpad + 32) * 4;
+  if (tile_bytes + per_warp > 48 * 1024) return cudaErrorInvalidValue;  // checked at set-up
+  const int wpb = std::max(1, std::min(8, (48 * 1024 - tile_bytes) / per_warp));
+  const size_t smem = static_cast<size_t>(tile_bytes) + static_cast<size_t>(per_warp) * wpb;
+  const unsigned grid = static_cast<unsigned>((nq + wpb - 1) / wpb);
+  const int ns = ix->n_starts, np = ix->n_probes;
+  const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
+  const int NPsel = np <= 1 ? 1 : (np <= 2 ? 2 : (np <= 4 ? 4 : 8));
+#define SONG_2L(M, NS, NP)                                                                                    \
+  nearest_entry_2level_kernel<M, NS, NP><<<grid, 32 * wpb, smem, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows,  \
+                                                                      ix->n_coarse, ix->d_entry_rows,          \
+                                                                      ix->d_entry_ids, ix->d_offsets, np, ns, out)
+#define SONG_2L_NP(M, NS)                 \
+  switch (NPsel) {                        \
+    case 1: SONG_2L(M, NS, 1); break;     \
+    case 2: SONG_2L(M, NS, 2); break;     \
+    case 4: SONG_2L(M, NS, 4); break;     \
+    default: SONG_2L(M, NS, 8); break;    \
+  }
+#define SONG_2L_NS(M)                     \
+  switch (NSel) {                         \
+    case 1: SONG_2L_NP(M, 1); break;      \
+    case 2: SONG_2L_NP(M, 2); break;      \
+    case 4: SONG_2L_NP(M, 4); break;      \
+    default: SONG_2L_NP(M, 8); break;     \
+  }
+  switch (ix->dx.metric) {
+    case SONG_METRIC_L2: SONG_2L_NS(SONG_METRIC_L2); break;
+    case SONG_METRIC_IP: SONG_2L_NS(SONG_METRIC_IP); break;
+    default: SONG_2L_NS(SONG_METRIC_COS); break;
+  }
+#undef SONG_2L_NS
+#undef SONG_2L_NP
+#undef SONG_2L
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+void clear_entries(song_index *ix) {
+  cudaFree(ix->d_entry_ids);
+  cudaFree(ix->d_entry_rows);
+  cudaFree(ix->d_coarse_rows);
+  cudaFree(ix->d_offsets);
+  ix->d_entry_ids = nullptr;
+  ix->d_entry_rows = nullptr;
+  ix->d_coarse_rows = nullptr;
+  ix->d_offsets = nullptr;
+  ix->n_entries = 0;
+  ix->n_coarse = 0;
+  ix->n_probes = 0;
+  ix->n_starts = 1;
+}
 
 int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s) {
   c.starts = nullptr;
@@ -334,41 +594,11 @@ int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s) {
     ix->cap_starts = need;
   }
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
-  // warps per block: up to 8, within the default 48 KB of shared memory;
-  // rows of up to 1 KB are staged through shared memory in 32-row tiles
-  const int qb = ix->dx.metric == SONG_METRIC_COS ? 1 : 2;
-  const int per_warp = static_cast<int>(sizeof(float)) * dpad * qb;
-  const int tile_bytes = 32 * (dpad / 4 + 1) * 16;
-  const bool tiled = dpad * 4 <= 1024 && tile_bytes + per_warp <= 48 * 1024;
-  const int avail = 48 * 1024 - (tiled ? tile_bytes : 0);
-  const int wpb = std::max(1, std::min(8, avail / per_warp));
-  const size_t smem = static_cast<size_t>(per_warp) * wpb + (tiled ? tile_bytes : 0);
-  const unsigned grid = static_cast<unsigned>((c.nq + wpb * qb - 1) / (wpb * qb));
-  const int ns = ix->n_starts;
-  const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
-#define SONG_ENTRY_LAUNCH(M, QB, NS)                                                                        \
-  do {                                                                                                   \
-    if (tiled)                                                                                           \
-      nearest_entry_tiled_kernel<M, QB, NS><<<grid, 32 * wpb, smem, s>>>(                                \
-          c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ns, ix->d_starts); \
-    else                                                                                                 \
-      nearest_entry_kernel<M, QB, NS><<<grid, 32 * wpb, smem, s>>>(                                      \
-          c.queries, c.nq, dim, dpad, ix->d_entry_rows, ix->d_entry_ids, ix->n_entries, ns, ix->d_starts); \
-  } while (0)
-#define SONG_ENTRY_BY_NS(M, QB)              \
-  switch (NSel) {                            \
-    case 1: SONG_ENTRY_LAUNCH(M, QB, 1); break; \
-    case 2: SONG_ENTRY_LAUNCH(M, QB, 2); break; \
-    case 4: SONG_ENTRY_LAUNCH(M, QB, 4); break; \
-    default: SONG_ENTRY_LAUNCH(M, QB, 8); break; \
-  }
-  switch (ix->dx.metric) {
-    case SONG_METRIC_L2: SONG_ENTRY_BY_NS(SONG_METRIC_L2, 2); break;
-    case SONG_METRIC_IP: SONG_ENTRY_BY_NS(SONG_METRIC_IP, 2); break;
-    default: SONG_ENTRY_BY_NS(SONG_METRIC_COS, 1); break;
-  }
-#undef SONG_ENTRY_BY_NS
-#undef SONG_ENTRY_LAUNCH
+  const cudaError_t le =
+      ix->n_coarse > 0 ? launch_2level(ix, c.queries, c.nq, ix->d_starts, s)
+                       : launch_nearest(c.queries, c.nq, dim, dim, dpad, ix->dx.metric, ix->d_entry_rows,
+                                        ix->d_entry_ids, ix->n_entries, ix->n_starts, ix->d_starts, s);
+  if (le != cudaSuccess) return fail(SONG_ERR_CUDA, "entry launch: %s", cudaGetErrorString(le));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "entry launch: %s", cudaGetErrorString(e));
   c.starts = ix->d_starts;
@@ -391,13 +621,14 @@ extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int c
     if (ids[i] >= ix->dx.n) return fail(SONG_ERR_ARG, "entry %d: id %llu >= n", i, (unsigned long long)ids[i]);
     h[i] = static_cast<uint32_t>(ids[i]);
   }
+  {
+    std::vector<uint32_t> u(h);
+    std::sort(u.begin(), u.end());
+    if (std::adjacent_find(u.begin(), u.end()) != u.end()) return fail(SONG_ERR_ARG, "entry ids must be distinct");
+  }
   cudaError_t e = cudaSetDevice(ix->device);
   if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
-  cudaFree(ix->d_entry_ids);
-  cudaFree(ix->d_entry_rows);
-  ix->d_entry_ids = nullptr;
-  ix->d_entry_rows = nullptr;
-  ix->n_entries = 0;
+  clear_entries(ix);
   if (count == 0) return SONG_OK;
   const int dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
   e = cudaMalloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
@@ -418,6 +649,125 @@ extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int c
     return fail(e == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "entries: %s", cudaGetErrorString(e));
   }
   ix->n_entries = count;
+  ix->n_starts = starts;
+  return SONG_OK;
+}
+
+extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids, int count, int coarse, int probes,
+                                             int starts) {
+  using namespace song;
+  clear_error();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (count < 1 || count > SONG_MAX_ENTRIES_2LEVEL || !ids)
+    return fail(SONG_ERR_ARG, "entry count must be 1..%d", SONG_MAX_ENTRIES_2LEVEL);
+  if (coarse < 1 || coarse > count || coarse > SONG_MAX_COARSE)
+    return fail(SONG_ERR_ARG, "coarse must be 1..min(count, %d)", SONG_MAX_COARSE);
+  if (probes < 1 || probes > SONG_MAX_STARTS || probes > coarse)
+    return fail(SONG_ERR_ARG, "probes must be 1..min(%d, coarse)", SONG_MAX_STARTS);
+  if (starts < 1 || starts > probes) return fail(SONG_ERR_ARG, "starts must be 1..probes");
+  const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
+  if (32 * (dpad / 4 + 1) * 16 + (dpad + 32) * 4 > 48 * 1024)
+    return fail(SONG_ERR_ARG, "two-level entries support rows of up to %d floats", 640);
+  std::vector<uint32_t> h(static_cast<size_t>(count));
+  for (int i = 0; i < count; ++i) {
+    if (ids[i] >= ix->dx.n) return fail(SONG_ERR_ARG, "entry %d: id %llu >= n", i, (unsigned long long)ids[i]);
+    h[i] = static_cast<uint32_t>(ids[i]);
+  }
+  {
+    std::vector<uint32_t> u(h);
+    std::sort(u.begin(), u.end());
+    if (std::adjacent_find(u.begin(), u.end()) != u.end()) return fail(SONG_ERR_ARG, "entry ids must be distinct");
+  }
+  cudaError_t e = cudaSetDevice(ix->device);
+  if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  clear_entries(ix);
+  // 1. all entry rows in list order; the clusters of the non-coarse entries
+  uint32_t *d_ids = nullptr, *d_assign = nullptr, *d_perm = nullptr;
+  float *d_rows = nullptr;
+  std::vector<uint32_t> assign(static_cast<size_t>(count - coarse));
+  e = cudaMalloc(&d_ids, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = cudaMalloc(&d_rows, sizeof(float) * static_cast<size_t>(count) * dpad);
+  if (e == cudaSuccess && count > coarse) e = cudaMalloc(&d_assign, sizeof(uint32_t) * (count - coarse));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_ids, h.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
+  if (e == cudaSuccess) {
+    gather_entry_rows_kernel<<<256, 256, 0, ix->stream>>>(ix->dx.rows_f32, static_cast<uint32_t>(dpad), d_ids, count,
+                                                          dpad, d_rows);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && count > coarse)
+    e = launch_nearest(d_rows + static_cast<size_t>(coarse) * dpad, count - coarse, dpad, dim, dpad, ix->dx.metric,
+                       d_rows, d_ids, coarse, 1, d_assign, ix->stream);
+  if (e == cudaSuccess && count > coarse)
+    e = cudaMemcpyAsync(assign.data(), d_assign, sizeof(uint32_t) * (count - coarse), cudaMemcpyDeviceToHost,
+                        ix->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
+  // 2. clusters numbered by coarse id; entries ordered by cluster
+  std::vector<int> corder(static_cast<size_t>(coarse));
+  for (int i = 0; i < coarse; ++i) corder[i] = i;
+  std::sort(corder.begin(), corder.end(), [&](int a, int b) { return h[a] < h[b]; });
+  std::vector<uint32_t> cl_of_id_sorted(static_cast<size_t>(coarse));  // sorted coarse ids
+  std::vector<int> rank(static_cast<size_t>(coarse));
+  for (int k = 0; k < coarse; ++k) {
+    rank[corder[k]] = k;
+    cl_of_id_sorted[k] = h[corder[k]];
+  }
+  std::vector<uint32_t> cluster(static_cast<size_t>(count));
+  for (int f = 0; f < count && e == cudaSuccess; ++f) {
+    if (f < coarse) {
+      cluster[f] = static_cast<uint32_t>(rank[f]);
+    } else {
+      const auto it = std::lower_bound(cl_of_id_sorted.begin(), cl_of_id_sorted.end(), assign[f - coarse]);
+      cluster[f] = static_cast<uint32_t>(it - cl_of_id_sorted.begin());
+    }
+  }
+  std::vector<uint32_t> offsets(static_cast<size_t>(coarse) + 1, 0u), perm(static_cast<size_t>(count)),
+      fine_ids(static_cast<size_t>(count)), cperm(static_cast<size_t>(coarse));
+  for (int f = 0; f < count; ++f) ++offsets[cluster[f] + 1];
+  for (int k = 0; k < coarse; ++k) offsets[k + 1] += offsets[k];
+  {
+    std::vector<uint32_t> fill(offsets.begin(), offsets.end() - 1);
+    for (int f = 0; f < count; ++f) {
+      const uint32_t pos = fill[cluster[f]]++;
+      perm[pos] = static_cast<uint32_t>(f);  // row f of d_rows
+      fine_ids[pos] = h[f];
+    }
+  }
+  for (int k = 0; k < coarse; ++k) cperm[k] = static_cast<uint32_t>(corder[k]);
+  // 3. device copies: entries in cluster order, coarse rows by id, offsets
+  uint32_t *d_cperm = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&d_perm, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = cudaMalloc(&d_cperm, sizeof(uint32_t) * coarse);
+  if (e == cudaSuccess) e = cudaMalloc(&ix->d_entry_rows, sizeof(float) * static_cast<size_t>(count) * dpad);
+  if (e == cudaSuccess) e = cudaMalloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = cudaMalloc(&ix->d_coarse_rows, sizeof(float) * static_cast<size_t>(coarse) * dpad);
+  if (e == cudaSuccess) e = cudaMalloc(&ix->d_offsets, sizeof(uint32_t) * (coarse + 1));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_perm, perm.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_cperm, cperm.data(), sizeof(uint32_t) * coarse, cudaMemcpyHostToDevice, ix->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ix->d_entry_ids, fine_ids.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ix->d_offsets, offsets.data(), sizeof(uint32_t) * (coarse + 1), cudaMemcpyHostToDevice,
+                        ix->stream);
+  if (e == cudaSuccess) {
+    gather_entry_rows_kernel<<<256, 256, 0, ix->stream>>>(d_rows, static_cast<uint32_t>(dpad), d_perm, count, dpad,
+                                                          ix->d_entry_rows);
+    gather_entry_rows_kernel<<<64, 256, 0, ix->stream>>>(d_rows, static_cast<uint32_t>(dpad), d_cperm, coarse, dpad,
+                                                         ix->d_coarse_rows);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
+  cudaFree(d_ids);
+  cudaFree(d_rows);
+  cudaFree(d_assign);
+  cudaFree(d_perm);
+  cudaFree(d_cperm);
+  if (e != cudaSuccess) {
+    clear_entries(ix);
+    return fail(e == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "entries: %s", cudaGetErrorString(e));
+  }
+  ix->n_entries = count;
+  ix->n_coarse = coarse;
+  ix->n_probes = probes;
   ix->n_starts = starts;
   return SONG_OK;
 }

@@ -97,6 +97,13 @@ struct song_index {
   float *d_entry_rows = nullptr;
   int n_entries = 0;
   int n_starts = 1;  // start vertices per query (nearest entries)
+  // two-level choice (n_coarse > 0): d_entry_rows / d_entry_ids hold all
+  // entries in cluster order, d_offsets the clusters, d_coarse_rows the
+  // coarse entries sorted by id
+  int n_coarse = 0;
+  int n_probes = 0;
+  float *d_coarse_rows = nullptr;
+  uint32_t *d_offsets = nullptr;
   uint32_t *d_starts = nullptr;
   size_t cap_starts = 0;
   uint64_t device_bytes = 0;

@@ -88,3 +88,45 @@ def test_entry_arguments_are_checked(song):
             ix.search(g["queries"][:3], 5, 5)
         ix.set_entries(np.array([n - 1], dtype=np.uint64))  # a single entry is allowed
         assert ix.search(g["queries"][:3], 20, 5).shape == (3, 5)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_two_level_entries_match_oracle(song, oracle, name):
+    """Two-level choice (song_index_set_entries_2level): the first `coarse`
+    entries are clusters, the rest join their nearest; each query searches
+    its `probes` nearest clusters.  Same starts and same search as the
+    oracle's orc_nearest_entry_2level + orc_kernel_search_from."""
+    g = load_golden(name)
+    shift, metric = int(g["shift"]), int(g["metric"])
+    ox = oracle.OracleIndex(g["data"], g["graph"], shift, metric)
+    rng = np.random.default_rng(9)
+    ent = rng.choice(g["data"].shape[0], 300, replace=False).astype(np.uint64)  # unsorted on purpose
+    for coarse, probes, ns in ((20, 4, 3), (7, 2, 2), (1, 1, 1)):
+        starts = ox.nearest_entry_2level(g["queries"], ent, coarse, probes, ns)
+        with song.Index(g["graph"], g["data"], shift, metric) as ix:
+            ix.set_entries(ent, starts=ns, coarse=coarse, probes=probes)
+            ids, hops, evals = ix.search(g["queries"], 60, 60, stats=True)
+        o_ids, o_hops, o_evals, _ = ox.kernel_search_from(g["queries"], starts, 60, oracle.MODE_LEX)
+        assert np.array_equal(ids, o_ids), (name, coarse, probes, ns)
+        assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
+
+
+def test_two_level_arguments_are_checked(song):
+    g = load_golden("l2_s5_d32")
+    with song.Index(g["graph"], g["data"], int(g["shift"]), int(g["metric"])) as ix:
+        ent = np.arange(40, dtype=np.uint64)
+        rc = song.load_library().song_index_set_entries_2level(ix._h, ent.ctypes.data, 40, 0, 1, 1)
+        assert rc == song.SONG_ERR_ARG  # no coarse entries
+        for bad in (dict(coarse=41, probes=1), dict(coarse=4, probes=5),
+                    dict(coarse=8, probes=2, starts=3)):
+            kw = dict(starts=1)
+            kw.update(bad)
+            with pytest.raises(song.SongError):
+                ix.set_entries(ent, **kw)
+        with pytest.raises(song.SongError):  # duplicate ids
+            ix.set_entries(np.array([3, 4, 3], dtype=np.uint64), starts=1, coarse=2, probes=1)
+        with pytest.raises(song.SongError):
+            ix.set_entries(np.array([3, 4, 3], dtype=np.uint64), starts=1)
+        ix.set_entries(ent, starts=2, coarse=8, probes=2)
+        assert ix.search(g["queries"][:4], 20, 5).shape == (4, 5)
+        ix.set_entries(None)
