@@ -35,7 +35,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PQ_SWEEP = [50, 75, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800, 1000]
+PQ_SWEEP = [40, 50, 60, 70, 80, 90, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800, 1000]
 CPU_K_SWEEP = [10, 20, 40, 80, 150, 300, 500, 800, 1200, 1600, 2000]
 
 
@@ -68,8 +68,11 @@ def parse_args():
                         "learned / plain / entries: that path only; "
                         "precision: storage error and recall table; serve: Poisson request stream; "
                         "build: graph construction, GPU searches vs the CPU builder")
-    p.add_argument("--entries", type=int, default=8192, help="entry vertices of the entries arm (sampled, seeded)")
+    p.add_argument("--entries", type=int, default=65536, help="entry vertices of the entries arm (sampled, seeded)")
     p.add_argument("--starts", type=int, default=4, help="start vertices per query: its nearest entries")
+    p.add_argument("--coarse", type=int, default=512,
+                   help="two-level entry choice: this many of the entries are cluster heads (0: flat)")
+    p.add_argument("--probes", type=int, default=4, help="clusters searched per query (two-level choice)")
     p.add_argument("--serve-rate", type=float, default=20000.0, help="mean offered queries/s (serve)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="length of each request stream (serve)")
     p.add_argument("--rerank", type=int, default=100, help="FP32 re-ranked candidates (BF16 path)")
@@ -385,10 +388,15 @@ def run_precision(args, torch, local):
         run = Runner(ix, dq, k, stream)
         starts = [("vertex 0", None)]
         if args.entries > 0:
-            starts.append(("nearest %d of %d entries" % (args.starts, args.entries),
-                           S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10)))
-        for start, ents in starts:
-            ix.set_entries(ents, starts=args.starts)
+            # two-level choice for rows of up to 640 floats, else a flat set of at most 8192
+            two = w.dim <= 640 and args.coarse > 0
+            n_ent = args.entries if two else min(args.entries, 8192)
+            starts.append(("nearest %d of %d entries%s" % (args.starts, n_ent, " (%d clusters, %d probed)"
+                                                           % (args.coarse, args.probes) if two else ""),
+                           (S.sample_entries(w.n, n_ent, seed=D.SEED_BASE + 10, shuffle=True), two)))
+        for start, ent_cfg in starts:
+            ents, two = ent_cfg if ent_cfg is not None else (None, False)
+            ix.set_entries(ents, starts=args.starts, coarse=args.coarse if two else 0, probes=args.probes)
             for rerank in ((0,) if storage == "f32" else (0, -1)):
                 if storage != "f32":
                     ix.set_rerank(rerank)
@@ -602,7 +610,8 @@ def main():
     ent = None
     if args.mode in ("best", "entries") and args.entries > 0:
         ixe = S.Index(graph, data, w.shift, w.metric, device=local)
-        ixe.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10), starts=args.starts)
+        ixe.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True), starts=args.starts,
+                        coarse=args.coarse, probes=args.probes)
         rune = Runner(ixe, dq, k, stream)
         pqe, sweepe = (args.pq, []) if args.pq else sweep_pq(torch, rune, w, data, queries, gt_kth, k, args.recall,
                                                               args.curve, "fp32+entries")
@@ -610,7 +619,8 @@ def main():
         rece = GT.recall_tie_aware(rune.ids(), data, queries, gt_kth, w.metric, k)
         mse = timed_steps(torch, rune, pqe, max(3, args.steps // 2), flush, stream)
         ent = {"qps": round(nq / (statistics.median(mse) / 1000.0), 1), "pq": pqe, "recall_at_10": round(rece, 4),
-               "entries": args.entries, "starts_per_query": args.starts, "kernel_ms_median": round(statistics.median(mse), 4),
+               "entries": args.entries, "starts_per_query": args.starts, "coarse": args.coarse,
+               "probes": args.probes, "kernel_ms_median": round(statistics.median(mse), 4),
                "mean_hops": round(float(rune.hops.float().mean().item()), 2),
                "mean_evals": round(float(rune.evals.float().mean().item()), 2), "pq_sweep_recall_qps": sweepe}
         log("[bench] FP32 from entries: %s" % ent)
@@ -621,7 +631,8 @@ def main():
         ix = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
         ix.set_rerank(args.rerank)
         if args.entries > 0:  # the same entry points as the entries arm (traces start there too)
-            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10), starts=args.starts)
+            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True),
+                           starts=args.starts, coarse=args.coarse, probes=args.probes)
         run = Runner(ix, dq, k, stream)
         train_q = D.query_vectors(w, nq=args.train_queries, seed=D.SEED_TRAIN)
         pq0 = min(pq32, ent["pq"]) if ent else pq32
@@ -759,7 +770,9 @@ def main():
         desc = {"learned": "learned early exit + BF16 storage + FP32 rerank"
                            + (", from the nearest %d of %d entry vertices" % (args.starts, args.entries)
                               if args.entries > 0 else ""),
-                "entries": "FP32 search from the nearest %d of %d entry vertices" % (args.starts, args.entries),
+                "entries": "FP32 search from the nearest %d of %d entry vertices%s" % (
+                    args.starts, args.entries,
+                    " (%d clusters, %d probed)" % (args.coarse, args.probes) if args.coarse else ""),
                 "plain": "plain FP32 search"}[mode]
         line = {
             "metric": "queries/s at recall@10>=%.2f, %s (%s)" % (args.recall, w.name, desc),

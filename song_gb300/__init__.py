@@ -307,10 +307,13 @@ def graph_build(data, metric, shift=5, search_degree=15, fixed_degree=31, budget
     return out
 
 
-def sample_entries(n, count=4096, seed=11):
-    """count distinct vertex ids drawn uniformly from 0..n-1 (seeded), sorted."""
+def sample_entries(n, count=4096, seed=11, shuffle=False):
+    """count distinct vertex ids drawn uniformly from 0..n-1 (seeded), sorted,
+    or in draw order with shuffle=True (then any prefix is itself a uniform
+    sample, e.g. the coarse entries of a two-level choice)."""
     rng = np.random.default_rng(seed)
-    return np.sort(rng.choice(n, min(count, n), replace=False)).astype(np.uint64)
+    ids = rng.choice(n, min(count, n), replace=False).astype(np.uint64)
+    return ids if shuffle else np.sort(ids)
 
 
 def graph_build_gpu(data, metric, shift=5, search_degree=15, fixed_degree=31, budget=150,
