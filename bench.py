@@ -35,7 +35,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PQ_SWEEP = [40, 50, 60, 70, 80, 90, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800, 1000]
+PQ_SWEEP = [40, 45, 50, 55, 60, 65, 70, 75, 80, 90, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800,
+            1000]
 CPU_K_SWEEP = [10, 20, 40, 80, 150, 300, 500, 800, 1200, 1600, 2000]
 
 
@@ -68,9 +69,9 @@ def parse_args():
                         "learned / plain / entries: that path only; "
                         "precision: storage error and recall table; serve: Poisson request stream; "
                         "build: graph construction, GPU searches vs the CPU builder")
-    p.add_argument("--entries", type=int, default=65536, help="entry vertices of the entries arm (sampled, seeded)")
+    p.add_argument("--entries", type=int, default=262144, help="entry vertices of the entries arm (sampled, seeded)")
     p.add_argument("--starts", type=int, default=4, help="start vertices per query: its nearest entries")
-    p.add_argument("--coarse", type=int, default=512,
+    p.add_argument("--coarse", type=int, default=2048,
                    help="two-level entry choice: this many of the entries are cluster heads (0: flat)")
     p.add_argument("--probes", type=int, default=4, help="clusters searched per query (two-level choice)")
     p.add_argument("--serve-rate", type=float, default=20000.0, help="mean offered queries/s (serve)")

@@ -372,11 +372,26 @@ __device__ __forceinline__ float entry_distance(const float4 *x4, const float4 *
   float t[32], l[32];
 #pragma unroll
   for (int i = 0; i < 32; ++i) t[i] = l[i] = 0.0f;
+  // Rows read from L2 are loaded one group of 32 dimensions ahead, so each
+  // group's loads are in flight while the previous group is summed.
+  float4 nxt[8];
+  if (GLOBAL) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) nxt[i] = i < d4 ? __ldg(x4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   for (int c0 = 0; c0 < d4; c0 += 8) {
+    float4 cur[8];
+    if (GLOBAL) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        cur[i] = nxt[i];
+        nxt[i] = c0 + 8 + i < d4 ? __ldg(x4 + c0 + 8 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       if (c0 + i < d4) {
-        const float4 xv = GLOBAL ? __ldg(x4 + c0 + i) : x4[c0 + i];
+        const float4 xv = GLOBAL ? cur[i] : x4[c0 + i];
         const float4 qv = q4[c0 + i];
         const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
         const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
