@@ -129,3 +129,36 @@ def test_trace_is_consistent_with_the_search(oracle, name):
         stag = np.rint(2.0 ** (tr[:, 2] * 10.0) - 1.0)
         changed = np.concatenate([[True], np.diff(tr[:, 5]) > 0])
         assert np.all(stag[changed] == 0) and np.all(stag[~changed] > 0)
+
+
+def test_two_level_entry_choice_follows_its_definition(oracle):
+    """orc_nearest_entry_2level against a direct restatement: heads are
+    ids[:coarse]; every other entry joins its nearest head; a query takes the
+    ns nearest entries of its `probes` nearest heads' clusters (ties to the
+    smaller id throughout); and the flat choice against brute force."""
+    g = load_golden("cos_s5_d26")
+    metric = int(g["metric"])
+    ox = oracle.OracleIndex(g["data"], g["graph"], int(g["shift"]), metric)
+    rng = np.random.default_rng(3)
+    ent = rng.choice(g["data"].shape[0], 120, replace=False).astype(np.uint64)
+    coarse, probes, ns = 9, 3, 2
+    q = g["queries"][:12]
+
+    def dist(qv, i):
+        return oracle.kernel_distance(metric, qv, g["data"][int(i)])
+
+    def nearest(qv, ids, m):
+        return sorted(ids, key=lambda i: (dist(qv, i), int(i)))[:m]
+
+    heads = list(ent[:coarse])
+    owner = {int(e): int(e) for e in heads}
+    for e in ent[coarse:]:
+        owner[int(e)] = int(nearest(g["data"][int(e)], heads, 1)[0])
+    got = ox.nearest_entry_2level(q, ent, coarse, probes, ns)
+    for i in range(q.shape[0]):
+        probed = set(int(h) for h in nearest(q[i], heads, probes))
+        cand = [e for e in ent if owner[int(e)] in probed]
+        assert [int(x) for x in got[i]] == [int(x) for x in nearest(q[i], cand, ns)]
+    flat = ox.nearest_entry(q, ent, ns=4)
+    for i in range(q.shape[0]):
+        assert [int(x) for x in flat[i]] == [int(x) for x in nearest(q[i], list(ent), 4)]
