@@ -168,8 +168,11 @@ int song_index_set_hop_limit(song_index *index, int max_hops);
  * rows, ties to the smaller id), chosen on the GPU before the search: they
  * enter the candidate queue and the visited set nearest first, and the search
  * itself is unchanged.  1 <= starts <= min(SONG_MAX_STARTS, count) and
- * starts <= pq.  count = 0 restores vertex 0.  song_search_noalloc and the
- * server always start at vertex 0.  No counterpart in the reference. */
+ * starts <= pq.  count = 0 restores vertex 0.  A server created on the
+ * index afterwards makes the same choice inside its persistent warps (its
+ * requests then need pq >= starts), and the entries cannot change while it
+ * exists.  song_search_noalloc always starts at vertex 0.  No counterpart in
+ * the reference. */
 #define SONG_MAX_ENTRIES 65536
 #define SONG_MAX_STARTS 8
 int song_index_set_entries(song_index *index, const uint64_t *ids, int count, int starts);

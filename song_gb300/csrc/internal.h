@@ -104,6 +104,7 @@ struct song_index {
   int n_probes = 0;
   float *d_coarse_rows = nullptr;
   uint32_t *d_offsets = nullptr;
+  int servers = 0;  // servers using the entries (song_server_create); they stay fixed meanwhile
   uint32_t *d_starts = nullptr;
   size_t cap_starts = 0;
   uint64_t device_bytes = 0;

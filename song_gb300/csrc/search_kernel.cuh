@@ -85,6 +85,16 @@ struct Params {
   int32_t *trace_final;   // [nq]: final top-k version, hops traced
   const uint32_t *starts; // [nq][n_starts] start vertices of each query, or null: vertex 0
   int n_starts;
+  // entry points chosen inside the server's persistent warps (entry_rows
+  // null: vertex 0); the layout of song_index's entry fields
+  const float *entry_rows;
+  const uint32_t *entry_ids;
+  int n_entries;
+  const float *coarse_rows;
+  int n_coarse;
+  const uint32_t *entry_offsets;
+  int n_probes;
+  int entry_dpad;
 };
 
 template <int METRIC>

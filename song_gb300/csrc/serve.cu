@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "entry_choice.cuh"
 #include "search_kernel.cuh"
 #include "song_gb300.h"
 
@@ -57,6 +58,65 @@ __device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t *p) {
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
   return *reinterpret_cast<const volatile uint32_t *>(p);
+}
+
+// The entry choice of entries.cu (flat or two-level, same definition, same
+// arithmetic) made by one warp for one query staged in qv (zero-padded to
+// entry_dpad floats): the p.n_starts starts, nearest first, into out[].
+template <int METRIC>
+__device__ __forceinline__ void serve_choose_starts(const Params &p, const float *qv, uint32_t *out, int lane) {
+  const int d4 = p.entry_dpad >> 2;
+  const float4 *q4 = reinterpret_cast<const float4 *>(qv);
+  constexpr int NL = 8;  // SONG_MAX_STARTS
+  float bd[NL];
+  uint32_t bi[NL];
+#pragma unroll
+  for (int m = 0; m < NL; ++m) {
+    bd[m] = __int_as_float(0x7f800000);
+    bi[m] = 0xffffffffu;
+  }
+  if (p.n_coarse > 0) {
+    // heads (sorted by id: the position is the tie order), then the clusters
+    float hd[NL];
+    uint32_t hi[NL];
+#pragma unroll
+    for (int m = 0; m < NL; ++m) {
+      hd[m] = __int_as_float(0x7f800000);
+      hi[m] = 0xffffffffu;
+    }
+    for (int c = lane; c < p.n_coarse; c += 32)
+      list_insert<NL>(hd, hi,
+                      entry_distance<METRIC, true>(
+                          reinterpret_cast<const float4 *>(p.coarse_rows + static_cast<size_t>(c) * p.entry_dpad), q4, d4),
+                      static_cast<uint32_t>(c));
+    int h = 0;
+    uint32_t mine = 0;
+    for (int r = 0; r < p.n_probes; ++r) {
+      const uint32_t c = list_take<NL>(hd, hi, h);
+      if (lane == r) mine = c;
+    }
+    for (int r = 0; r < p.n_probes; ++r) {
+      const uint32_t c = __shfl_sync(FULL, mine, r);
+      const uint32_t end = p.entry_offsets[c + 1];
+      for (uint32_t e = p.entry_offsets[c] + lane; e < end; e += 32)
+        list_insert<NL>(bd, bi,
+                        entry_distance<METRIC, true>(
+                            reinterpret_cast<const float4 *>(p.entry_rows + static_cast<size_t>(e) * p.entry_dpad), q4, d4),
+                        p.entry_ids[e]);
+    }
+  } else {
+    for (int e = lane; e < p.n_entries; e += 32)
+      list_insert<NL>(bd, bi,
+                      entry_distance<METRIC, true>(
+                          reinterpret_cast<const float4 *>(p.entry_rows + static_cast<size_t>(e) * p.entry_dpad), q4, d4),
+                      p.entry_ids[e]);
+  }
+  int h = 0;
+  for (int r = 0; r < p.n_starts; ++r) {
+    const uint32_t id = list_take<NL>(bd, bi, h);
+    if (lane == 0) out[r] = id;
+  }
+  __syncwarp();
 }
 
 template <int METRIC, int STORAGE, int H, int S>
@@ -114,7 +174,16 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1)
     (void)ld_acquire_sys(&ctl->published);  // every lane: order the entry's and query's reads
     const ServeEntry e = ring[idx & ring_mask];
     QueryStats st;
-    if (!run_query<METRIC, STORAGE, H, S, false>(p, w, reinterpret_cast<const float *>(e.query), nullptr, 1, e.pq, e.k,
+    const uint32_t *starts = nullptr;
+    if (p.entry_rows) {  // entry points: the starts go to the candidate buffer, which run_query reads first
+      const float *qsrc = reinterpret_cast<const float *>(e.query);
+      for (int j = lane; j < p.entry_dpad; j += 32) w.qv[j] = j < p.dim ? qsrc[j] : 0.0f;
+      __syncwarp();
+      serve_choose_starts<METRIC>(p, w.qv, w.cbuf, lane);
+      starts = w.cbuf;
+    }
+    if (!run_query<METRIC, STORAGE, H, S, false>(p, w, reinterpret_cast<const float *>(e.query), starts,
+                                                 p.n_starts, e.pq, e.k,
                                                  reinterpret_cast<uint64_t *>(e.out), nullptr, st, lane)) {
       if (lane == 0) atomicOr(p.error, 1);
       return;
@@ -207,6 +276,7 @@ struct song_server {
   uint32_t ring_mask = 0;
   uint32_t published = 0;
   bool running = false;
+  bool holds_entries = false;  // counted in ix->servers: the index's entries stay fixed
   uint64_t next_ticket = 1;
   std::vector<Slot> slots;
   std::deque<Pending> pending;
@@ -342,6 +412,20 @@ int song_server_create(song_index *ix, int max_pq, int max_k, int nslots, int sl
   p.shift = dx.shift;
   p.dim = dim;
   p.error = ix->d_error;
+  p.n_starts = 1;
+  if (ix->n_entries > 0) {  // the index's entry points, fixed for the server's life
+    p.entry_rows = ix->d_entry_rows;
+    p.entry_ids = ix->d_entry_ids;
+    p.n_entries = ix->n_entries;
+    p.coarse_rows = ix->d_coarse_rows;
+    p.n_coarse = ix->n_coarse;
+    p.entry_offsets = ix->d_offsets;
+    p.n_probes = ix->n_probes;
+    p.n_starts = ix->n_starts;
+    p.entry_dpad = static_cast<int>(dx.f32_row_bytes / 4);
+    ++ix->servers;
+    s->holds_entries = true;
+  }
   uint32_t off = 2u * s->H * dx.row_bytes;
   off = song::align_up(off, 16);
   p.off_mbar = off;
@@ -373,6 +457,7 @@ int song_server_submit(song_server *s, const float *queries, int nq, int pq, int
   if (!s || !queries || !ticket) return fail(SONG_ERR_ARG, "null argument");
   if (nq < 1 || nq > s->slot_queries) return fail(SONG_ERR_ARG, "nq must be in [1, %d]", s->slot_queries);
   if (pq < 2 || pq > s->max_pq || k < 1 || k > pq || k > s->max_k) return fail(SONG_ERR_ARG, "bad pq or k");
+  if (pq < s->params.n_starts) return fail(SONG_ERR_ARG, "pq must be at least the %d entry starts", s->params.n_starts);
   std::lock_guard<std::mutex> lk(s->mu);
   int prev = -1;
   cudaGetDevice(&prev);
@@ -472,6 +557,7 @@ int song_server_destroy(song_server *s) {
   cudaFreeHost(s->h_ctl);
   cudaFreeHost(s->h_done);
   cudaFree(s->d_next);
+  if (s->holds_entries) --s->ix->servers;
   if (s->ix && prev >= 0 && prev != s->ix->device) cudaSetDevice(prev);
   delete s;
   return SONG_OK;

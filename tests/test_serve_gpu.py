@@ -57,6 +57,47 @@ def test_two_indexes_in_the_mix_equal_alone(song):
             ix.free()
 
 
+@pytest.mark.parametrize("two_level", [False, True])
+def test_server_with_entry_points_equals_search(song, two_level):
+    """With entry points on the index, the server's warps choose each query's
+    starts themselves; the ids must equal song_search's (whose starts come
+    from the pre-pass kernels) on the same index, and the entries stay fixed
+    while the server exists."""
+    import time
+    from song_gb300.serve import Server
+    rng = np.random.default_rng(1)
+    g = load_golden("l2_s5_d32" if two_level else "cos_s5_d26")
+    ix = song.Index(g["graph"], g["data"], int(g["shift"]), int(g["metric"]))
+    ent = rng.choice(g["data"].shape[0], 256, replace=False).astype(np.uint64)
+    if two_level:
+        ix.set_entries(ent, starts=3, coarse=16, probes=4)
+    else:
+        ix.set_entries(ent, starts=3)
+    reqs = _requests(rng, 30, g["queries"].shape[0], (10, 50, 100), (1, 10))
+    alone = [ix.search(g["queries"][s:s + n], pq, k) for (s, n, pq, k) in reqs]
+    srv = Server(ix, max_pq=100, max_k=10, slots=4, slot_queries=64, sm_fraction=0.5)
+    try:
+        with pytest.raises(song.SongError):  # the server holds the entries
+            ix.set_entries(None)
+        with pytest.raises(song.SongError):  # pq below the number of starts
+            srv.submit(g["queries"][:1], 2, 1)
+        pending = {srv.submit(g["queries"][s:s + n], pq, k): ri for ri, (s, n, pq, k) in enumerate(reqs)}
+        got = [None] * len(reqs)
+        t0 = time.time()
+        while pending and time.time() - t0 < 60:
+            for t in srv.poll():
+                ri = pending.pop(t)
+                s, n, pq, k = reqs[ri]
+                got[ri] = srv.result(t, n, k)
+        assert not pending, "requests not completed"
+        for ri in range(len(reqs)):
+            assert np.array_equal(got[ri], alone[ri]), ri
+    finally:
+        srv.close()
+    ix.set_entries(None)  # released with the server
+    ix.free()
+
+
 def test_poisson_stream_results_and_latency(song, capsys):
     from song_gb300 import datasets as D
     from song_gb300.serve import Server, poisson_stream
