@@ -447,13 +447,23 @@ def run_serve(args, torch, local):
     import song_gb300 as S
     from song_gb300 import datasets as D
     from song_gb300.serve import Server, poisson_stream
-    servers, indexes, qsets, names = [], [], [], []
+    servers, indexes, qsets, names, starts_desc = [], [], [], [], []
     for name in ("scale-1m-128d-l2", "precision-1m-960d-cos"):
         a = argparse.Namespace(**vars(args))
         a.workload = name
         a.nq = 0
         w, data, queries, graph = load_workload(a)
         ix = S.Index(graph, data, w.shift, w.metric, device=local)
+        if w.dim <= 640 and args.entries > 0 and args.coarse > 0:
+            # two-level entry points, chosen by the server's warps; the 960-d
+            # index keeps vertex 0 (a choice over its rows costs more than it saves)
+            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True),
+                           starts=args.starts, coarse=args.coarse, probes=args.probes)
+            names_start = "%s: nearest %d of %d entries (%d clusters, %d probed)" % (
+                name, args.starts, args.entries, args.coarse, args.probes)
+        else:
+            names_start = "%s: vertex 0" % name
+        starts_desc.append(names_start)
         indexes.append(ix)
         qsets.append(D.query_vectors(w, nq=max(w.n_queries, 4096)))
         names.append(name)
@@ -479,6 +489,7 @@ def run_serve(args, torch, local):
     for s in servers:
         s.close()
     for ix in indexes:
+        ix.set_entries(None)
         ix.free()
     main_run = runs[str(int(args.serve_rate))]
     line = {"metric": "p99 request latency at a %.0f queries/s Poisson stream, 1M x 128 L2 + 1M x 960 cos resident"
@@ -490,6 +501,7 @@ def run_serve(args, torch, local):
                        "request": "1-256 queries log-uniform, k in {1,10,100}, pq in {50,100,200,400} (pq>=k)",
                        "admission": "64 slots x 256 queries per index (queue memory bound), "
                                     "persistent kernel per index on half the SMs",
+                       "starts": starts_desc,
                        "p50_ms": main_run["p50_ms"], "throughput_qps": main_run["throughput_qps"],
                        "load_sweep": runs},
             "e2e": {"value": main_run["throughput_qps"], "unit": "queries/s",
