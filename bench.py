@@ -6,18 +6,27 @@ over the resident index.  Default workload: 1,000,000 x 128 float32 vectors
 with integer values 0-255 (1,000-centre Gaussian mixture, sigma 20; a
 synthetic stand-in for SIFT1M's shape), L2, degree-32 graph (shift 5,
 FIXED_DEGREE 31, SEARCH_DEGREE 15) built by this project's batch-parallel
-builder, pq_size chosen as the smallest in a sweep whose recall@10 against an
-FP64 exact kNN reaches the target (0.95), top-10 returned.
+builder, top-10, recall@10 against an FP64 exact kNN (tie-aware).
 
-  value  queries/s of the kernel, queries and index resident in HBM, CUDA
-         events on the launching stream, L2 flushed between steps.
+The default mode measures three arms, each at the smallest pq of a sweep
+whose recall@10 reaches the target (0.95), and reports the fastest:
+  plain    the search from vertex 0 (the reference's semantics, FP32 rows);
+  entries  the same search from each query's nearest entry vertices
+           (two-level choice over sampled entries, song_index_set_entries_2level);
+  learned  the learned early exit with BF16 rows and FP32 rerank, from the
+           same entries.
+
+  value  queries/s of the reported arm's kernels, queries and index resident
+         in HBM, CUDA events on the launching stream, L2 flushed between steps.
   e2e    queries/s through song_search (host query buffer in pinned memory,
          host->device copy, search, device->host copy of the ids), host clock.
 
 `--impl reference` times the reference's CPU best-first search
 (graph.h:169-216; the oracle's restatement, pinned to the reference's own
 code by tests/golden) on all host cores, at the result size k whose recall@10
-matches the target, on bounded samples of the same workload.
+matches the target, on bounded samples of the same workload.  Other modes:
+precision (storage error and recall per row format), serve (Poisson request
+stream against two resident indexes), build (graph construction, GPU vs CPU).
 """
 from __future__ import annotations
 
