@@ -6,7 +6,7 @@ budget's finish rule, warp_astar_accelerator.h:191).  The network reads the
 query's state after each hop and stops the search once it is confident that
 the current top-k is already the final one; a query it never trusts runs the
 plain search unchanged, so the plain search is both the fallback and, through
-the labels, the judge.
+the labels, the reference the exit is trained against.
 
 Label of a hop: "the top-k set after this hop equals the top-k set the plain
 search returns" (the trace records how many times the top-k set has changed,
