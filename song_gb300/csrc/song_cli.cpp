@@ -16,7 +16,12 @@
 // SONG_PQ_SIZE when set.  Graph constants follow KernelFixedDegreeGraph
 // (kernelgraph.h:27-29: shift 5, degree 15, row capacity 31) unless
 // SONG_SHIFT / SONG_SEARCH_DEGREE / SONG_FIXED_DEGREE are set.
-// SONG_BUILD_DIV > 0 selects the batch-parallel build.
+// SONG_BUILD_DIV > 0 selects the batch-parallel build, SONG_BUILD_GPU=1 its
+// searches on GPU 0 (the same graph).  Test mode starts at vertex 0, as the
+// reference does, unless SONG_ENTRIES > 0: then each query starts from its
+// SONG_STARTS (default 4) nearest of SONG_ENTRIES vertices drawn with seed
+// SONG_ENTRY_SEED (default 11); SONG_COARSE > 0 makes the choice two-level
+// with SONG_PROBES (default 4) clusters probed.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -85,6 +90,26 @@ void usage(char **argv) {
 
 }  // namespace
 
+// count distinct ids of 0..n-1 in draw order: a partial Fisher-Yates shuffle
+// driven by splitmix64 from `seed` (any prefix is a uniform sample).
+std::vector<uint64_t> sample_ids(uint64_t n, int count, uint64_t seed) {
+  if (static_cast<uint64_t>(count) > n) count = static_cast<int>(n);
+  std::vector<uint64_t> perm(n);
+  for (uint64_t i = 0; i < n; ++i) perm[i] = i;
+  uint64_t x = seed;
+  for (int i = 0; i < count; ++i) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const uint64_t j = static_cast<uint64_t>(i) + z % (n - static_cast<uint64_t>(i));
+    std::swap(perm[i], perm[j]);
+  }
+  perm.resize(static_cast<size_t>(count));
+  return perm;
+}
+
 int main(int argc, char **argv) {
   if (argc != 9) {
     usage(argv);
@@ -117,9 +142,12 @@ int main(int argc, char **argv) {
     densify(rows, dim, row, data);
     std::vector<uint64_t> graph(static_cast<size_t>(row) << shift);
     fprintf(stderr, "Writing the graph and data...");
-    int rc = song_graph_build(data.data(), row, dim, metric, shift, search_degree, fixed_degree, 150,
-                              env_int("SONG_BUILD_DIV", 0),
-                              static_cast<int>(std::thread::hardware_concurrency()), graph.data());
+    const int nthreads = static_cast<int>(std::thread::hardware_concurrency());
+    int rc = env_int("SONG_BUILD_GPU", 0)
+                 ? song_graph_build_gpu(data.data(), row, dim, metric, shift, search_degree, fixed_degree, 150,
+                                        env_int("SONG_BUILD_DIV", 0), 0, nthreads, graph.data())
+                 : song_graph_build(data.data(), row, dim, metric, shift, search_degree, fixed_degree, 150,
+                                    env_int("SONG_BUILD_DIV", 0), nthreads, graph.data());
     if (rc) {
       fprintf(stderr, "\n%s: %s\n", song_status_string(rc), song_last_error());
       return 1;
@@ -155,6 +183,19 @@ int main(int argc, char **argv) {
     std::vector<float> q;
     densify(rows, dim, rows.size(), q);
     const int pq = env_int("SONG_PQ_SIZE", atoi(argv[4]));
+    const int n_entries = env_int("SONG_ENTRIES", 0);
+    if (n_entries > 0) {
+      const std::vector<uint64_t> ent = sample_ids(row, n_entries, static_cast<uint64_t>(env_int("SONG_ENTRY_SEED", 11)));
+      const int coarse = env_int("SONG_COARSE", 0);
+      rc = coarse > 0 ? song_index_set_entries_2level(ix, ent.data(), static_cast<int>(ent.size()), coarse,
+                                                      env_int("SONG_PROBES", 4), env_int("SONG_STARTS", 4))
+                      : song_index_set_entries(ix, ent.data(), static_cast<int>(ent.size()), env_int("SONG_STARTS", 4));
+      if (rc) {
+        fprintf(stderr, "%s: %s\n", song_status_string(rc), song_last_error());
+        song_index_free(ix);
+        return 1;
+      }
+    }
     const int nq = static_cast<int>(rows.size());
     std::vector<uint64_t> out(static_cast<size_t>(nq) * pq);
     rc = song_search(ix, q.data(), nq, pq, pq, out.data(), nullptr, nullptr);
