@@ -398,9 +398,9 @@ def run_precision(args, torch, local):
         run = Runner(ix, dq, k, stream)
         starts = [("vertex 0", None)]
         if args.entries > 0:
-            # two-level choice for rows of up to 640 floats, else a flat set of at most 8192
+            # two-level choice for rows of up to 640 floats, else a flat set of at most 4096
             two = w.dim <= 640 and args.coarse > 0
-            n_ent = args.entries if two else min(args.entries, 8192)
+            n_ent = args.entries if two else min(args.entries, 4096)
             starts.append(("nearest %d of %d entries%s" % (args.starts, n_ent, " (%d clusters, %d probed)"
                                                            % (args.coarse, args.probes) if two else ""),
                            (S.sample_entries(w.n, n_ent, seed=D.SEED_BASE + 10, shuffle=True), two)))
