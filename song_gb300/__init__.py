@@ -11,6 +11,12 @@ Reference surface mirrored here (sunbelbd/song):
                              (warp_astar_accelerator.h:347-423)
   * graph_build           <- FixedDegreeGraph::add_vertex loop (graph.h:149-167, main.cu:15-18)
   * read/write bfsg files <- Data::dump/load, *Graph::dump/load (data.h:164-175, kernelgraph.h:255-267)
+
+Additions without a reference counterpart: graph_build_gpu (the builder's
+searches on the GPU, same graph), Index.set_entries (queries start from their
+nearest entry vertices instead of vertex 0; flat or two-level choice), BF16 /
+FP8 storage with FP32 rerank, the learned early exit (learned.py), the
+continuous-batching server (serve.py) and search_noalloc.
 """
 from __future__ import annotations
 
@@ -24,6 +30,8 @@ from .build import LIB_PATH
 SONG_OK, SONG_ERR_ARG, SONG_ERR_OOM, SONG_ERR_TIMEOUT, SONG_ERR_CUDA, SONG_ERR_IO = range(6)
 SONG_MAX_ENTRIES = 65536  # include/song_gb300.h
 SONG_MAX_STARTS = 8
+SONG_MAX_ENTRIES_2LEVEL = 1 << 20
+SONG_MAX_COARSE = 16384
 METRICS = {"l2": 0, "ip": 1, "cos": 2}
 STORAGES = {"f32": 0, "bf16": 1, "fp8": 2}
 MAX_PQ = 1023
