@@ -1,7 +1,7 @@
 """FP64 NumPy restatement of the early-exit network's objective and gradient.
 
-TEST INFRASTRUCTURE ONLY: the checker for the hand-written CUDA training
-kernels (song_gb300/csrc/mlp.cu).  Network 5 -> 32 -> 32 -> 1 with ReLU
+TEST INFRASTRUCTURE ONLY: the CPU restatement that the hand-written CUDA training
+kernels (song_gb300/csrc/mlp.cu) are compared with.  Network 5 -> 32 -> 32 -> 1 with ReLU
 (derivative 0 at 0), loss = sum_i w_i (softplus(z_i) - y_i z_i) / sum_i w_i,
 parameters in the SONG_MLP_PARAMS layout W1[32][5], b1[32], W2[32][32],
 b2[32], w3[32], b3.

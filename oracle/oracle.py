@@ -2,7 +2,7 @@
 harness (oracle/ref_harness.cpp -> oracle/_ref/).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
-the cpu_baseline / reference legs of bench.py, always as the checker or the
+the cpu_baseline / reference legs of bench.py, always as the correctness reference or the
 timed CPU baseline, never by the product package.
 """
 from __future__ import annotations

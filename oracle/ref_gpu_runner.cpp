@@ -5,7 +5,7 @@
 // 347-423): data, graph and densified queries uploaded, <<<nq, 32>>>, ids
 // copied back.
 //
-// TEST INFRASTRUCTURE ONLY: the checker for the FMA assumption of the oracle
+// TEST INFRASTRUCTURE ONLY: the test of the FMA assumption of the oracle
 // and the reference GPU baseline.  Built on the GPU host by oracle/ref_gpu.py.
 //
 // Safety: the kernel allocates its queues and visited hash with device-side

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (song_gb300/, include/)
  * links, imports or calls this code; only tests/, __graft_entry__.smoke() and
- * the cpu_baseline / reference legs of bench.py do, and only as the checker or
+ * the cpu_baseline / reference legs of bench.py do, and only as the correctness reference or
  * the timed CPU baseline.
  *
  * It restates, in plain C, three algorithms of sunbelbd/song:
