@@ -13,7 +13,10 @@
 // computes a whole distance: it keeps the 32 partial sums, adds each element
 // to the partial of its lane in dimension order, and then adds them in the
 // butterfly's pairs, which gives every lane's (identical) result.  The entry
-// rows are copied once into a contiguous block, which stays in L2.
+// rows are copied once into a contiguous block, which stays in L2.  The
+// cluster phase of the two-level choice instead spreads each row over the
+// warp as the search does and adds the partials in a transposed butterfly
+// (warp_rows_distance): the same sums, read with coalesced loads.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -362,12 +365,88 @@ cudaError_t launch_nearest(const float *queries, int nq, int qstride, int dim, i
 // entries of their clusters.
 // ---------------------------------------------------------------------------
 
+// The search distances of rows base .. base+nr-1 (nr <= 32) to the staged
+// query qw (dpad floats), computed by the whole warp; lane l returns row
+// base+l's.  Lane l reads dimensions l, l+32, ... of every row, so each read
+// is one coalesced line per row, and keeps the FMA partial sum of those
+// dimensions, which is partial l of entry_distance.  A transposed xor
+// butterfly then adds the 32 rows' partials in the butterfly's pairs: at the
+// step with offset o a lane keeps the half of its rows selected by bit o of
+// its lane number and adds the partner's partials of that half, so after the
+// last step lane l holds row l's sum, bit for bit entry_distance's.
+template <int METRIC>
+__device__ __forceinline__ float warp_rows_distance(const float *rows, int dpad, uint32_t base, int nr,
+                                                    const float *qw, int lane) {
+  constexpr int U = 4;  // rows whose loads are issued together
+  float t[32], l[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) t[i] = l[i] = 0.0f;
+#pragma unroll
+  for (int u0 = 0; u0 < 32; u0 += U) {
+    if (u0 < nr) {
+      const float *r0 = rows + static_cast<size_t>(base + u0) * dpad;
+      for (int j = 0; 32 * j < dpad; j += 4) {
+        float qv[4], x[U][4];
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int d = lane + 32 * (j + jj);
+          qv[jj] = d < dpad ? qw[d] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int d = lane + 32 * (j + jj);
+            x[u][jj] = (u0 + u < nr && d < dpad) ? __ldg(r0 + static_cast<size_t>(u) * dpad + d) : 0.0f;
+          }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int d = lane + 32 * (j + jj);
+            if (u0 + u < nr && d < dpad) {
+              if (METRIC == SONG_METRIC_L2) {
+                const float df = __fsub_rn(qv[jj], x[u][jj]);
+                t[u0 + u] = __fmaf_rn(df, df, t[u0 + u]);
+              } else {
+                t[u0 + u] = __fmaf_rn(qv[jj], x[u][jj], t[u0 + u]);
+                if (METRIC == SONG_METRIC_COS) l[u0 + u] = __fmaf_rn(x[u][jj], x[u][jj], l[u0 + u]);
+              }
+            }
+          }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < o; ++i) {
+      const float ts = up ? t[i] : t[i + o];
+      const float tk = up ? t[i + o] : t[i];
+      t[i] = __fadd_rn(tk, __shfl_xor_sync(0xffffffffu, ts, o));
+      if (METRIC == SONG_METRIC_COS) {
+        const float ls = up ? l[i] : l[i + o];
+        const float lk = up ? l[i + o] : l[i];
+        l[i] = __fadd_rn(lk, __shfl_xor_sync(0xffffffffu, ls, o));
+      }
+    }
+  }
+  if (METRIC == SONG_METRIC_L2) return t[0];
+  if (METRIC == SONG_METRIC_IP) return -t[0];
+  if (l[0] != 0.0f) {
+    const float sign = t[0] < 0.0f ? 1.0f : -1.0f;
+    return __fdiv_rn(__fmul_rn(__fmul_rn(sign, t[0]), t[0]), l[0]);
+  }
+  return 0.0f;
+}
+
 // One warp per query.  Phase 1 streams the coarse rows (sorted by id, so the
 // position is the tie order) through shared-memory tiles shared by the
 // block; phase 2 reads the probed clusters' rows (cluster-ordered block in
-// L2), each lane a row.
+// L2) 32 at a time with warp_rows_distance.
 template <int METRIC, int NS, int NP>
-__global__ void __launch_bounds__(256) nearest_entry_2level_kernel(const float *queries, int nq, int dim, int dpad,
+__global__ void __launch_bounds__(256, METRIC == SONG_METRIC_L2 && NS <= 4 ? 3 : 2) nearest_entry_2level_kernel(const float *queries, int nq, int dim, int dpad,
                                                                    const float *coarse_rows, int n_coarse,
                                                                    const float *fine_rows, const uint32_t *fine_ids,
                                                                    const uint32_t *offsets, int probes, int ns,
@@ -418,10 +497,10 @@ __global__ void __launch_bounds__(256) nearest_entry_2level_kernel(const float *
   for (int r = 0; r < probes; ++r) {
     const uint32_t c = pw[r];
     const uint32_t end = offsets[c + 1];
-    for (uint32_t e = offsets[c] + lane; e < end; e += 32) {
-      const float d = entry_distance<METRIC, true>(reinterpret_cast<const float4 *>(fine_rows + static_cast<size_t>(e) * dpad),
-                                                   q4, d4);
-      list_insert<NS>(bd, bi, d, fine_ids[e]);
+    for (uint32_t b = offsets[c]; b < end; b += 32) {
+      const int nr = static_cast<int>(min(32u, end - b));
+      const float d = warp_rows_distance<METRIC>(fine_rows, dpad, b, nr, qw, lane);
+      if (lane < nr) list_insert<NS>(bd, bi, d, fine_ids[b + lane]);
     }
   }
   h = 0;
