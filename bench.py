@@ -828,7 +828,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(nq * w.dim * 4),
                     "d2h_bytes_per_step": int(nq * k * 8)},
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * (1 + (0 if mode == "plain" or args.entries <= 0
+                                                else (2 if args.coarse > 0 else 1))),
             "clocks": clocks,
             "kernel_ms": {"min": round(min(kernel_ms), 4), "median": round(statistics.median(kernel_ms), 4),
                           "max": round(max(kernel_ms), 4)},

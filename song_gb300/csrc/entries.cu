@@ -441,27 +441,37 @@ __device__ __forceinline__ float warp_rows_distance(const float *rows, int dpad,
   return 0.0f;
 }
 
-// One warp per query.  Phase 1 streams the coarse rows (sorted by id, so the
-// position is the tie order) through shared-memory tiles shared by the
-// block; phase 2 reads the probed clusters' rows (cluster-ordered block in
-// L2) 32 at a time with warp_rows_distance.
-template <int METRIC, int NS, int NP>
-__global__ void __launch_bounds__(256, METRIC == SONG_METRIC_L2 && NS <= 4 ? 3 : 2) nearest_entry_2level_kernel(const float *queries, int nq, int dim, int dpad,
-                                                                   const float *coarse_rows, int n_coarse,
-                                                                   const float *fine_rows, const uint32_t *fine_ids,
-                                                                   const uint32_t *offsets, int probes, int ns,
-                                                                   uint32_t *starts) {
+// 16-byte global-to-shared copies that complete without holding registers
+// (cp.async, waited for by group).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Two-level choice, first kernel: every query's `probes` nearest coarse
+// entries.  One warp per query; the block streams the coarse rows (sorted by
+// id, so the position is the tie order) through shared-memory tiles of 32
+// rows, lane e scoring row e of the tile.  With nbuf == 2 the next tile's
+// copies are in flight while the current tile is scored.
+template <int METRIC, int NP>
+__global__ void __launch_bounds__(256) nearest_head_kernel(const float *queries, int nq, int dim, int dpad,
+                                                           const float *coarse_rows, int n_coarse, int probes,
+                                                           int nbuf, uint32_t *probe_out) {
   extern __shared__ float4 sm4[];
   constexpr int TILE = 32;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int qi = blockIdx.x * nwarps + wib;
   const bool active = qi < nq;
-  const int d4 = dpad >> 2, rs4 = d4 + 1;
-  float4 *tile = sm4;
-  float *qw = reinterpret_cast<float *>(sm4 + TILE * rs4) + static_cast<size_t>(wib) * (dpad + 32);
-  uint32_t *pw = reinterpret_cast<uint32_t *>(qw + dpad);  // this warp's probed clusters (<= 8)
+  const int d4 = dpad >> 2, rs4 = d4 + 1, tile_elems = TILE * rs4;
+  float *qw = reinterpret_cast<float *>(sm4 + nbuf * tile_elems) + static_cast<size_t>(wib) * dpad;
   for (int j = lane; j < dpad; j += 32) qw[j] = (active && j < dim) ? queries[static_cast<size_t>(qi) * dim + j] : 0.0f;
   const float4 *q4 = reinterpret_cast<const float4 *>(qw);
+  const float4 *src4 = reinterpret_cast<const float4 *>(coarse_rows);
   float pd[NP];
   uint32_t pi[NP];
 #pragma unroll
@@ -469,23 +479,58 @@ __global__ void __launch_bounds__(256, METRIC == SONG_METRIC_L2 && NS <= 4 ? 3 :
     pd[m] = __int_as_float(0x7f800000);
     pi[m] = 0xffffffffu;
   }
-  for (int t0 = 0; t0 < n_coarse; t0 += TILE) {
+  auto issue = [&](int t0, float4 *buf) {
     const int rows = min(TILE, n_coarse - t0);
-    __syncthreads();
     for (int i = threadIdx.x; i < rows * d4; i += blockDim.x) {
       const int r = i / d4, c = i - r * d4;
-      tile[r * rs4 + c] = __ldg(reinterpret_cast<const float4 *>(coarse_rows + static_cast<size_t>(t0 + r) * dpad) + c);
+      cp_async16(buf + r * rs4 + c, src4 + static_cast<size_t>(t0 + r) * d4 + c);
     }
-    __syncthreads();
+    cp_async_commit();
+  };
+  if (nbuf == 2) issue(0, sm4);
+  for (int t0 = 0, k = 0; t0 < n_coarse; t0 += TILE, ++k) {
+    float4 *cur = sm4 + (nbuf == 2 ? (k & 1) * tile_elems : 0);
+    if (nbuf == 2) {
+      // the other buffer was last read before the previous iteration's closing barrier
+      if (t0 + TILE < n_coarse) {
+        issue(t0 + TILE, sm4 + ((k + 1) & 1) * tile_elems);
+      } else {
+        cp_async_commit();
+      }
+      cp_async_wait<1>();  // this thread's copies of the current tile have landed
+    } else {
+      issue(t0, cur);
+      cp_async_wait<0>();
+    }
+    __syncthreads();  // ... and every thread's, as has the staged query
+    const int rows = min(TILE, n_coarse - t0);
     if (active && lane < rows)
-      list_insert<NP>(pd, pi, entry_distance<METRIC, false>(tile + lane * rs4, q4, d4), static_cast<uint32_t>(t0 + lane));
+      list_insert<NP>(pd, pi, entry_distance<METRIC, false>(cur + lane * rs4, q4, d4), static_cast<uint32_t>(t0 + lane));
+    __syncthreads();
   }
   if (!active) return;
   int h = 0;
   for (int r = 0; r < probes; ++r) {
     const uint32_t c = list_take<NP>(pd, pi, h);
-    if (lane == 0) pw[r] = c;
+    if (lane == 0) probe_out[static_cast<size_t>(qi) * probes + r] = c;
   }
+}
+
+// Two-level choice, second kernel: the ns nearest entries of each query's
+// probed clusters (cluster-ordered block in L2), 32 rows at a time with
+// warp_rows_distance.  Warps are independent (no barrier), so blocks are
+// small and a query with large clusters holds only its own warp's slot.
+template <int METRIC, int NS>
+__global__ void __launch_bounds__(64, METRIC == SONG_METRIC_L2 && NS <= 4 ? 12 : 8)
+    nearest_in_clusters_kernel(const float *queries, int nq, int dim, int dpad, const float *fine_rows,
+                               const uint32_t *fine_ids, const uint32_t *offsets, const uint32_t *probe_in,
+                               int probes, int ns, uint32_t *starts) {
+  extern __shared__ float qs[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (qi >= nq) return;  // whole warps leave together
+  float *qw = qs + static_cast<size_t>(wib) * dpad;
+  for (int j = lane; j < dpad; j += 32) qw[j] = j < dim ? queries[static_cast<size_t>(qi) * dim + j] : 0.0f;
   __syncwarp();
   float bd[NS];
   uint32_t bi[NS];
@@ -495,7 +540,7 @@ __global__ void __launch_bounds__(256, METRIC == SONG_METRIC_L2 && NS <= 4 ? 3 :
     bi[m] = 0xffffffffu;
   }
   for (int r = 0; r < probes; ++r) {
-    const uint32_t c = pw[r];
+    const uint32_t c = probe_in[static_cast<size_t>(qi) * probes + r];
     const uint32_t end = offsets[c + 1];
     for (uint32_t b = offsets[c]; b < end; b += 32) {
       const int nr = static_cast<int>(min(32u, end - b));
@@ -503,50 +548,57 @@ __global__ void __launch_bounds__(256, METRIC == SONG_METRIC_L2 && NS <= 4 ? 3 :
       if (lane < nr) list_insert<NS>(bd, bi, d, fine_ids[b + lane]);
     }
   }
-  h = 0;
+  int h = 0;
   for (int r = 0; r < ns; ++r) {
     const uint32_t id = list_take<NS>(bd, bi, h);
     if (lane == 0) starts[static_cast<size_t>(qi) * ns + r] = id;
   }
 }
 
+// Both kernels on stream s.  `out` holds nq * (ns + probes) words: the
+// starts, then the probed clusters.
 cudaError_t launch_2level(const song_index *ix, const float *queries, int nq, uint32_t *out, cudaStream_t s) {
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
   const int tile_bytes = 32 * (dpad / 4 + 1) * 16;
-  const int per_warp = (dpad + 32) * 4;
+  const int per_warp = dpad * 4;
   if (tile_bytes + per_warp > 48 * 1024) return cudaErrorInvalidValue;  // checked at set-up
-  const int wpb = std::max(1, std::min(8, (48 * 1024 - tile_bytes) / per_warp));
-  const size_t smem = static_cast<size_t>(tile_bytes) + static_cast<size_t>(per_warp) * wpb;
-  const unsigned grid = static_cast<unsigned>((nq + wpb - 1) / wpb);
+  const int nbuf = 2 * tile_bytes + per_warp <= 48 * 1024 ? 2 : 1;
+  const int wpb = std::max(1, std::min(8, (48 * 1024 - nbuf * tile_bytes) / per_warp));
+  const size_t smem_a = static_cast<size_t>(nbuf) * tile_bytes + static_cast<size_t>(per_warp) * wpb;
+  const unsigned grid_a = static_cast<unsigned>((nq + wpb - 1) / wpb);
   const int ns = ix->n_starts, np = ix->n_probes;
+  uint32_t *probes = out + static_cast<size_t>(nq) * ns;
   const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
   const int NPsel = np <= 1 ? 1 : (np <= 2 ? 2 : (np <= 4 ? 4 : 8));
-#define SONG_2L(M, NS, NP)                                                                                    \
-  nearest_entry_2level_kernel<M, NS, NP><<<grid, 32 * wpb, smem, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows,  \
-                                                                      ix->n_coarse, ix->d_entry_rows,          \
-                                                                      ix->d_entry_ids, ix->d_offsets, np, ns, out)
-#define SONG_2L_NP(M, NS)                 \
-  switch (NPsel) {                        \
-    case 1: SONG_2L(M, NS, 1); break;     \
-    case 2: SONG_2L(M, NS, 2); break;     \
-    case 4: SONG_2L(M, NS, 4); break;     \
-    default: SONG_2L(M, NS, 8); break;    \
-  }
-#define SONG_2L_NS(M)                     \
-  switch (NSel) {                         \
-    case 1: SONG_2L_NP(M, 1); break;      \
-    case 2: SONG_2L_NP(M, 2); break;      \
-    case 4: SONG_2L_NP(M, 4); break;      \
-    default: SONG_2L_NP(M, 8); break;     \
+  const unsigned grid_b = static_cast<unsigned>((nq + 1) / 2);
+  const size_t smem_b = static_cast<size_t>(per_warp) * 2;
+#define SONG_HEADS(M, NP)                                                                                   \
+  nearest_head_kernel<M, NP><<<grid_a, 32 * wpb, smem_a, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows, \
+                                                               ix->n_coarse, np, nbuf, probes)
+#define SONG_CLUSTERS(M, NS)                                                                              \
+  nearest_in_clusters_kernel<M, NS><<<grid_b, 64, smem_b, s>>>(queries, nq, dim, dpad, ix->d_entry_rows, \
+                                                                ix->d_entry_ids, ix->d_offsets, probes, np, ns, out)
+#define SONG_2L(M)                          \
+  switch (NPsel) {                          \
+    case 1: SONG_HEADS(M, 1); break;        \
+    case 2: SONG_HEADS(M, 2); break;        \
+    case 4: SONG_HEADS(M, 4); break;        \
+    default: SONG_HEADS(M, 8); break;       \
+  }                                         \
+  switch (NSel) {                           \
+    case 1: SONG_CLUSTERS(M, 1); break;     \
+    case 2: SONG_CLUSTERS(M, 2); break;     \
+    case 4: SONG_CLUSTERS(M, 4); break;     \
+    default: SONG_CLUSTERS(M, 8); break;    \
   }
   switch (ix->dx.metric) {
-    case SONG_METRIC_L2: SONG_2L_NS(SONG_METRIC_L2); break;
-    case SONG_METRIC_IP: SONG_2L_NS(SONG_METRIC_IP); break;
-    default: SONG_2L_NS(SONG_METRIC_COS); break;
+    case SONG_METRIC_L2: SONG_2L(SONG_METRIC_L2); break;
+    case SONG_METRIC_IP: SONG_2L(SONG_METRIC_IP); break;
+    default: SONG_2L(SONG_METRIC_COS); break;
   }
-#undef SONG_2L_NS
-#undef SONG_2L_NP
 #undef SONG_2L
+#undef SONG_CLUSTERS
+#undef SONG_HEADS
   return cudaGetLastError();
 }
 
@@ -572,7 +624,8 @@ int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s) {
   c.n_starts = 1;
   if (ix->n_entries <= 0 || c.nq <= 0) return SONG_OK;
   if (ix->n_starts > c.pq) return fail(SONG_ERR_ARG, "%d start vertices need pq >= %d", ix->n_starts, ix->n_starts);
-  const size_t need = static_cast<size_t>(c.nq) * ix->n_starts;
+  // the starts, then (two-level choice) each query's probed clusters
+  const size_t need = static_cast<size_t>(c.nq) * (ix->n_starts + (ix->n_coarse > 0 ? ix->n_probes : 0));
   if (need > ix->cap_starts) {
     if (ix->d_starts) cudaFree(ix->d_starts);
     ix->d_starts = nullptr;

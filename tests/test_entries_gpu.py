@@ -111,6 +111,30 @@ def test_two_level_entries_match_oracle(song, oracle, name):
         assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
 
 
+@pytest.mark.parametrize("dim,metric", [(200, 0), (200, 1), (200, 2), (130, 0)])
+def test_two_level_wide_rows_match_oracle(song, oracle, dim, metric):
+    """Rows wider than 128 floats: the cluster kernel's warp reads several
+    32-float groups per row (one partial group at 130), and at 200 floats two
+    coarse tiles no longer fit the head kernel's shared memory, so it stages
+    one tile at a time.  Clusters of ~75 rows take several 32-row batches."""
+    from song_gb300 import datasets as D
+    shift = 5
+    data = D.mixture("unit", 700, dim, 8, seed=dim + metric, center_seed=dim + 50)
+    q = D.mixture("unit", 40, dim, 8, seed=dim + metric + 1, center_seed=dim + 50)
+    graph = song.graph_build(data, metric, shift, 15, 31, 150, batch_div=0, nthreads=1)
+    ox = oracle.OracleIndex(data, graph, shift, metric)
+    rng = np.random.default_rng(dim)
+    ent = rng.choice(700, 300, replace=False).astype(np.uint64)
+    for coarse, probes, ns in ((20, 4, 3), (4, 2, 2)):
+        starts = ox.nearest_entry_2level(q, ent, coarse, probes, ns)
+        with song.Index(graph, data, shift, metric) as ix:
+            ix.set_entries(ent, starts=ns, coarse=coarse, probes=probes)
+            ids, hops, evals = ix.search(q, 40, 40, stats=True)
+        o_ids, o_hops, o_evals, _ = ox.kernel_search_from(q, starts, 40, oracle.MODE_LEX)
+        assert np.array_equal(ids, o_ids), (dim, metric, coarse, probes, ns)
+        assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
+
+
 def test_two_level_arguments_are_checked(song):
     g = load_golden("l2_s5_d32")
     with song.Index(g["graph"], g["data"], int(g["shift"]), int(g["metric"])) as ix:
