@@ -271,7 +271,7 @@ def run_reference(args, rank, world):
         total_t += dt
     value = total_q / total_t
     line = {
-        "impl": "reference", "metric": "queries/s at recall@10>=%.2f" % args.recall, "value": round(value, 1),
+        "impl": "reference", "metric": "queries/s at recall@10>=%.2f, %s" % (args.recall, w.name), "value": round(value, 1),
         "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * total_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64-accumulated f32", "data": "synthetic",
@@ -797,13 +797,13 @@ def main():
                     " (%d clusters, %d probed)" % (args.coarse, args.probes) if args.coarse else ""),
                 "plain": "plain FP32 search"}[mode]
         line = {
-            "metric": "queries/s at recall@10>=%.2f, %s (%s)" % (args.recall, w.name, desc),
+            "metric": "queries/s at recall@10>=%.2f, %s" % (args.recall, w.name),
             "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": wsteps, "ms_per_step": round(1000 * total_s / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 storage, f32 accumulate, f32 rerank" if mode == "learned" else "f32",
             "data": "synthetic (seeded Gaussian mixture, SIFT1M shape)",
-            "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric,
+            "config": {"workload": w.name, "arm": desc, "n": w.n, "dim": w.dim, "metric": w.metric,
                        "graph": "shift %d (FIXED_DEGREE %d, SEARCH_DEGREE %d), batch-parallel build div %d"
                                 % (w.shift, w.fixed_degree, w.search_degree, args.build_div),
                        "mode": mode, "pq": pq, "top_k": k, "queries_per_step": nq,
