@@ -100,7 +100,10 @@ int song_search(song_index *index, const float *queries, int nq, int pq, int k, 
                 int32_t *hops, int32_t *evals);
 
 /* Batched search with DEVICE buffers, enqueued on `stream` (a cudaStream_t,
- * NULL = the legacy default stream) without synchronising. */
+ * NULL = the legacy default stream) without synchronising.  Searches of one
+ * index must not overlap on the device (issue them on one stream, or order
+ * the streams): they share the index's work counter, error flag and, with
+ * entry points set, its buffer of chosen starts. */
 int song_search_device(song_index *index, const float *d_queries, int nq, int pq, int k,
                        uint64_t *d_out, int32_t *d_hops, int32_t *d_evals, void *stream);
 
