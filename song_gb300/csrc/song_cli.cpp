@@ -22,6 +22,19 @@
 // SONG_STARTS (default 4) nearest of SONG_ENTRIES vertices drawn with seed
 // SONG_ENTRY_SEED (default 11); SONG_COARSE > 0 makes the choice two-level
 // with SONG_PROBES (default 4) clusters probed.
+//
+// Binary I/O (no reference counterpart; the reference parses LIBSVM text,
+// parser.h:48-64): SONG_DATA_FORMAT=f32 makes build read <build_data> and
+// SONG_QUERY_FORMAT=f32 makes test read <query_data> as raw little-endian
+// float32 rows, the bfsg.data layout (the row count is the file size over
+// 4 * dim); SONG_RESULTS=<file> makes test write nq x return_top_k
+// little-endian uint64 ids (UINT64_MAX where a query has fewer) to <file>
+// instead of printing the lines.
+//
+//   song convert <libsvm_in> <dim> <f32_out>
+//
+// writes a LIBSVM file's vectors as float32 rows, densified as test and build
+// densify them.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -83,9 +96,62 @@ void densify(const std::vector<std::vector<std::pair<int, float>>> &rows, int di
     for (const auto &p : rows[i]) out[i * dim + p.first] = p.second;
 }
 
+// Raw little-endian float32 rows of dim floats; n = file size / (4 dim).
+bool read_f32_rows(const char *path, int dim, std::vector<float> &out, size_t &n, std::string &err) {
+  FILE *fp = fopen(path, "rb");
+  if (!fp) {
+    err = std::string("File not found at (") + path + ")";
+    return false;
+  }
+  const size_t row_bytes = sizeof(float) * static_cast<size_t>(dim > 0 ? dim : 0);
+  long long size = -1;
+  if (fseek(fp, 0, SEEK_END) == 0) size = ftell(fp);
+  if (dim <= 0 || size < 0 || fseek(fp, 0, SEEK_SET) != 0 || static_cast<size_t>(size) % row_bytes != 0) {
+    fclose(fp);
+    err = std::string(path) + ": size is not a whole number of rows of dim float32";
+    return false;
+  }
+  n = static_cast<size_t>(size) / row_bytes;
+  out.assign(n * static_cast<size_t>(dim), 0.0f);
+  const size_t got = n ? fread(out.data(), row_bytes, n, fp) : 0;
+  fclose(fp);
+  if (got != n) {
+    err = std::string(path) + ": short read";
+    return false;
+  }
+  return true;
+}
+
+// SONG_DATA_FORMAT / SONG_QUERY_FORMAT: "libsvm" (default) or "f32"; -1 otherwise.
+int input_format(const char *name) {
+  const char *v = getenv(name);
+  if (!v || !*v || strcmp(v, "libsvm") == 0) return 0;
+  return strcmp(v, "f32") == 0 ? 1 : -1;
+}
+
+// The rows of a LIBSVM or float32 file; with rows >= 0 zero-padded or cut to
+// that many (build densifies to <row>), else all of them.
+bool read_rows(const char *path, int dim, int format, long long rows, std::vector<float> &out, size_t &n,
+               std::string &err) {
+  if (format == 1) {
+    if (!read_f32_rows(path, dim, out, n, err)) return false;
+  } else {
+    std::vector<std::vector<std::pair<int, float>>> sparse;
+    if (!parse_libsvm(path, dim, sparse, err)) return false;
+    n = sparse.size();
+    densify(sparse, dim, n, out);
+  }
+  if (rows >= 0) {
+    out.resize(static_cast<size_t>(rows) * static_cast<size_t>(dim), 0.0f);
+    n = static_cast<size_t>(rows);
+  }
+  return true;
+}
+
 void usage(char **argv) {
-  printf("Usage: %s <build/test> <build_data> <query_data> <search_top_k> <row> <dim> <return_top_k> <l2/ip/cos>\n",
-         argv[0]);
+  printf("Usage: %s <build/test> <build_data> <query_data> <search_top_k> <row> <dim> <return_top_k> <l2/ip/cos>\n"
+         "       %s convert <libsvm_in> <dim> <f32_out>\n",
+         argv[0], argv[0]);
 }
 
 }  // namespace
@@ -111,6 +177,24 @@ std::vector<uint64_t> sample_ids(uint64_t n, int count, uint64_t seed) {
 }
 
 int main(int argc, char **argv) {
+  if (argc == 5 && strcmp(argv[1], "convert") == 0) {
+    const int dim = atoi(argv[3]);
+    std::string err = "dim must be positive";
+    std::vector<float> v;
+    size_t n = 0;
+    if (dim <= 0 || !read_rows(argv[2], dim, 0, -1, v, n, err)) {
+      fprintf(stderr, "%s\n", err.c_str());
+      return 1;
+    }
+    FILE *fo = fopen(argv[4], "wb");
+    bool ok = fo && (n == 0 || fwrite(v.data(), sizeof(float) * dim, n, fo) == n);
+    if (fo && fclose(fo) != 0) ok = false;
+    if (!ok) {
+      fprintf(stderr, "cannot write %s\n", argv[4]);
+      return 1;
+    }
+    return 0;
+  }
   if (argc != 9) {
     usage(argv);
     return 1;
@@ -133,13 +217,14 @@ int main(int argc, char **argv) {
   const int fixed_degree = env_int("SONG_FIXED_DEGREE", (1 << shift) - 1);
   std::string err;
   if (mode == "build") {
-    std::vector<std::vector<std::pair<int, float>>> rows;
-    if (!parse_libsvm(argv[2], dim, rows, err)) {
+    const int fmt = input_format("SONG_DATA_FORMAT");
+    std::vector<float> data;
+    size_t n_read = 0;
+    if (fmt < 0) err = "SONG_DATA_FORMAT must be libsvm or f32";
+    if (fmt < 0 || !read_rows(argv[2], dim, fmt, static_cast<long long>(row), data, n_read, err)) {
       fprintf(stderr, "%s\n", err.c_str());
       return 1;
     }
-    std::vector<float> data;
-    densify(rows, dim, row, data);
     std::vector<uint64_t> graph(static_cast<size_t>(row) << shift);
     fprintf(stderr, "Writing the graph and data...");
     const int nthreads = static_cast<int>(std::thread::hardware_concurrency());
@@ -174,14 +259,15 @@ int main(int argc, char **argv) {
       return 1;
     }
     fprintf(stderr, "done\n");
-    std::vector<std::vector<std::pair<int, float>>> rows;
-    if (!parse_libsvm(argv[3], dim, rows, err)) {
-      fprintf(stderr, "%s\n", err.c_str());
+    const int fmt = input_format("SONG_QUERY_FORMAT");
+    std::vector<float> q;
+    size_t n_q = 0;
+    if (fmt < 0) err = "SONG_QUERY_FORMAT must be libsvm or f32";
+    if (fmt < 0 || !read_rows(argv[3], dim, fmt, -1, q, n_q, err) || n_q > 0x7fffffff) {
+      fprintf(stderr, "%s\n", n_q > 0x7fffffff ? "too many queries" : err.c_str());
       song_index_free(ix);
       return 1;
     }
-    std::vector<float> q;
-    densify(rows, dim, rows.size(), q);
     const int pq = env_int("SONG_PQ_SIZE", atoi(argv[4]));
     const int n_entries = env_int("SONG_ENTRIES", 0);
     if (n_entries > 0) {
@@ -196,13 +282,28 @@ int main(int argc, char **argv) {
         return 1;
       }
     }
-    const int nq = static_cast<int>(rows.size());
+    const int nq = static_cast<int>(n_q);
     std::vector<uint64_t> out(static_cast<size_t>(nq) * pq);
     rc = song_search(ix, q.data(), nq, pq, pq, out.data(), nullptr, nullptr);
     song_index_free(ix);
     if (rc) {
       fprintf(stderr, "%s: %s\n", song_status_string(rc), song_last_error());
       return 1;
+    }
+    const char *results = getenv("SONG_RESULTS");
+    if (results && *results) {
+      const int show = display > 0 ? display : 0;
+      std::vector<uint64_t> ids(static_cast<size_t>(nq) * show, UINT64_MAX);
+      for (int i = 0; i < nq; ++i)
+        for (int j = 0; j < pq && j < show; ++j) ids[static_cast<size_t>(i) * show + j] = out[static_cast<size_t>(i) * pq + j];
+      FILE *fo = fopen(results, "wb");
+      bool ok = fo && (ids.empty() || fwrite(ids.data(), sizeof(uint64_t), ids.size(), fo) == ids.size());
+      if (fo && fclose(fo) != 0) ok = false;
+      if (!ok) {
+        fprintf(stderr, "cannot write %s\n", results);
+        return 1;
+      }
+      return 0;
     }
     for (int i = 0; i < nq; ++i) {
       for (int j = 0; j < pq && j < display; ++j) {

@@ -67,3 +67,23 @@ def test_cli_test_mode_prints_the_oracle_ids(song, oracle, tmp_path, entries):
         o_ids = ox.kernel_search(queries, pq, oracle.MODE_LEX)[0]
     for i, line in enumerate(lines):
         assert [int(x) for x in line.split()] == [int(x) for x in o_ids[i, :show]], i
+
+
+def test_cli_binary_queries_and_results(song, oracle, tmp_path):
+    """SONG_QUERY_FORMAT=f32 + SONG_RESULTS: float32 query rows in, nq x
+    return_top_k uint64 ids out (UINT64_MAX beyond pq), the oracle's ids."""
+    g = load_golden("l2_s5_d32")
+    data, queries = g["data"], g["queries"]
+    data.astype(np.float32).tofile(str(tmp_path / "bfsg.data"))
+    g["graph"].astype(np.uint64).tofile(str(tmp_path / "bfsg.graph"))
+    queries.astype(np.float32).tofile(str(tmp_path / "q.f32"))
+    pq, show = 20, 25
+    r = _run(["test", "0", "q.f32", str(pq), str(data.shape[0]), str(data.shape[1]), str(show), "l2"],
+             tmp_path, SONG_QUERY_FORMAT="f32", SONG_RESULTS="ids.u64")
+    assert r.returncode == 0, r.stderr
+    assert r.stdout == ""
+    got = np.fromfile(str(tmp_path / "ids.u64"), dtype=np.uint64).reshape(queries.shape[0], show)
+    ox = oracle.OracleIndex(data, g["graph"], int(g["shift"]), int(g["metric"]))
+    o_ids = np.asarray(ox.kernel_search(queries, pq, oracle.MODE_LEX)[0], dtype=np.uint64)
+    assert np.array_equal(got[:, :pq], o_ids[:, :pq])
+    assert np.all(got[:, pq:] == np.uint64(0xFFFFFFFFFFFFFFFF))
