@@ -85,3 +85,32 @@ def test_batched_builder_is_deterministic_and_valid(song):
     for r in rows[:200]:
         ids = r[1:1 + int(r[0])]
         assert (ids < n).all()
+
+
+def test_header_is_plain_c(song, tmp_path):
+    """include/song_gb300.h compiles as strict C99 and links against the
+    library: every declared function is addressable from C, and the status
+    calls work without a GPU."""
+    import shutil
+    import subprocess
+    from song_gb300.build import LIB_DIR
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = header_functions()
+    src = tmp_path / "abi.c"
+    src.write_text(
+        "#include \"song_gb300.h\"\n#include <string.h>\n"
+        "typedef void (*fn)(void);\n"
+        "static fn table[] = {\n" + ",\n".join("  (fn)%s" % n for n in names) + "\n};\n"
+        "int main(void) {\n"
+        "  size_t i;\n"
+        "  for (i = 0; i < sizeof table / sizeof table[0]; ++i) if (!table[i]) return 2;\n"
+        "  return strcmp(song_status_string(SONG_OK), \"ok\") != 0;\n"
+        "}\n")
+    exe = tmp_path / "abi"
+    r = subprocess.run([cc, "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                        str(src), "-L" + LIB_DIR, "-lsong_gb300", "-Wl,-rpath," + LIB_DIR, "-o", str(exe)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)], timeout=60).returncode == 0
