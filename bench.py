@@ -398,8 +398,8 @@ def run_precision(args, torch, local):
         run = Runner(ix, dq, k, stream)
         starts = [("vertex 0", None)]
         if args.entries > 0:
-            # two-level choice for rows of up to 640 floats, else a flat set of at most 4096
-            two = w.dim <= 640 and args.coarse > 0
+            # two-level choice for rows of up to 364 floats, else a flat set of at most 4096
+            two = w.dim <= 364 and args.coarse > 0
             n_ent = args.entries if two else min(args.entries, 4096)
             starts.append(("nearest %d of %d entries%s" % (args.starts, n_ent, " (%d clusters, %d probed)"
                                                            % (args.coarse, args.probes) if two else ""),
@@ -463,7 +463,7 @@ def run_serve(args, torch, local):
         a.nq = 0
         w, data, queries, graph = load_workload(a)
         ix = S.Index(graph, data, w.shift, w.metric, device=local)
-        if w.dim <= 640 and args.entries > 0 and args.coarse > 0:
+        if w.dim <= 364 and args.entries > 0 and args.coarse > 0:
             # two-level entry points, chosen by the server's warps; the 960-d
             # index keeps vertex 0 (a choice over its rows costs more than it saves)
             ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True),

@@ -708,8 +708,14 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
     return fail(SONG_ERR_ARG, "probes must be 1..min(%d, coarse)", SONG_MAX_STARTS);
   if (starts < 1 || starts > probes) return fail(SONG_ERR_ARG, "starts must be 1..probes");
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
-  if (32 * (dpad / 4 + 1) * 16 + (dpad + 32) * 4 > 48 * 1024)
-    return fail(SONG_ERR_ARG, "two-level entries support rows of up to %d floats", 640);
+  // the head kernel's 32-row tile (rows padded to an odd number of 16-byte
+  // units) and one staged query fit 48 KB of shared memory
+  auto fits = [](int dp) { return 32 * (dp / 4 + 1) * 16 + (dp + 32) * 4 <= 48 * 1024; };
+  if (!fits(dpad)) {
+    int widest = 4;
+    while (fits(widest + 4)) widest += 4;
+    return fail(SONG_ERR_ARG, "two-level entries support rows of up to %d floats", widest);
+  }
   std::vector<uint32_t> h(static_cast<size_t>(count));
   for (int i = 0; i < count; ++i) {
     if (ids[i] >= ix->dx.n) return fail(SONG_ERR_ARG, "entry %d: id %llu >= n", i, (unsigned long long)ids[i]);
