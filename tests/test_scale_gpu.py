@@ -77,6 +77,7 @@ def test_full_scale_entry_points_reach_the_recall_target(song, scale):
         dq = torch.from_numpy(np.ascontiguousarray(queries)).cuda()
         out = torch.empty((queries.shape[0], 10), dtype=torch.int64, device="cuda")
         stream = torch.cuda.Stream()
+        torch.cuda.synchronize()  # the upload above ran on another stream
         ix.search_device(dq.data_ptr(), queries.shape[0], 55, 10, out.data_ptr(), None, None, stream.cuda_stream)
         stream.synchronize()
         assert np.array_equal(out.cpu().numpy().view(np.uint64), ids)
