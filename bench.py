@@ -68,7 +68,7 @@ def parse_args():
     p.add_argument("--build-div", type=int, default=64)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cache", default=os.environ.get("SONG_CACHE", "/tmp/song_gb300_cache"))
+    p.add_argument("--cache", default=os.environ.get("SONG_CACHE", os.path.join(ROOT, "_cache")))
     p.add_argument("--curve", action="store_true", help="time every pq of the sweep (recall/throughput curve)")
     p.add_argument("--mode", choices=["best", "learned", "plain", "entries", "precision", "serve", "build"],
                    default="best",

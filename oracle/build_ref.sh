@@ -1,11 +1,11 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/ from the reference's own sources, where they lie.
-# TEST INFRASTRUCTURE ONLY; needs the reference tree (REF_DIR, default
-# /root/reference), which exists only in the development container.
+# TEST INFRASTRUCTURE ONLY; needs the reference source tree, named by the
+# REF_DIR environment variable (required; nothing is built without it).
 # Outputs go to oracle/_ref/ and nowhere else; the reference tree is only read.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_DIR="${REF_DIR:-/root/reference}"
+REF_DIR="${REF_DIR:?set REF_DIR to the reference source tree}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF_DIR/graph.h" ]; then
   echo "reference tree not found at $REF_DIR; oracle/_ref not built" >&2

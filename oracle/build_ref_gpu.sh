@@ -1,8 +1,8 @@
 #!/usr/bin/env bash
 # Rebuilds the reference's GPU search kernel (warp_astar_accelerator.h:41-341)
 # for sm_100, one cubin per (metric, dim, pq_size), into oracle/_ref/.
-# TEST INFRASTRUCTURE ONLY; needs the reference tree (REF_DIR, default
-# /root/reference), present only in the development container.
+# TEST INFRASTRUCTURE ONLY; needs the reference source tree, named by the
+# REF_DIR environment variable (required; nothing is built without it).
 #
 # The reference fixes TOPK (= pq_size) and DIM at compile time with its
 # template step (generate_template.sh:16-34, fill_parameters.sh:35-53: sed of
@@ -14,7 +14,7 @@
 # and with that line removed.  The reference tree itself is only read.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF_DIR="${REF_DIR:-/root/reference}"
+REF_DIR="${REF_DIR:?set REF_DIR to the reference source tree}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF_DIR/warp_astar_accelerator.h" ]; then
   echo "reference tree not found at $REF_DIR; reference cubins not built" >&2

@@ -84,7 +84,7 @@ def lib():
         L.orc_kernel_search_from.restype = i32
         L.orc_kernel_search_from.argtypes = [P, P, i32, P, i32, i32, i32, i32, P, P, P, P, i32]
         L.orc_nearest_entry_2level.restype = i32
-        L.orc_nearest_entry_2level.argtypes = [P, P, i32, P, i32, i32, i32, i32, i32, P]
+        L.orc_nearest_entry_2level.argtypes = [P, P, i32, P, i32, i32, i32, i32, i32, P, i32]
         L.orc_nearest_entry.restype = i32
         L.orc_nearest_entry.argtypes = [P, P, i32, P, i32, i32, i32, P]
         L.orc_kernel_search_trace.restype = i32
@@ -169,13 +169,13 @@ class OracleIndex:
             raise ValueError("orc_nearest_entry failed")
         return out[:, 0].copy() if ns == 1 else out
 
-    def nearest_entry_2level(self, queries, entries, coarse, probes, ns, use_fma=True):
+    def nearest_entry_2level(self, queries, entries, coarse, probes, ns, use_fma=True, nthreads=None):
         """Two-level entry choice (orc_nearest_entry_2level): nq x ns."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         e = np.ascontiguousarray(entries, dtype=np.uint64)
         out = np.empty((q.shape[0], ns), dtype=np.uint64)
         if lib().orc_nearest_entry_2level(self.ref, _ptr(q), q.shape[0], _ptr(e), e.size, coarse, probes, ns,
-                                          int(use_fma), _ptr(out)) != 0:
+                                          int(use_fma), _ptr(out), nthreads or default_threads()) != 0:
             raise ValueError("orc_nearest_entry_2level failed")
         return out
 

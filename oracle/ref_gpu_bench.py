@@ -24,7 +24,7 @@ def main():
     ap.add_argument("--pq", default="100,200,400,600,800,1000")
     ap.add_argument("--repeats", type=int, default=3)
     ap.add_argument("--build-div", type=int, default=64)
-    ap.add_argument("--cache", default=os.environ.get("SONG_CACHE", "/tmp/song_gb300_cache"))
+    ap.add_argument("--cache", default=os.environ.get("SONG_CACHE", os.path.join(ROOT, "_cache")))
     a = ap.parse_args()
     import bench
     from oracle import ref_gpu

@@ -987,54 +987,132 @@ int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const u
  * nearest coarse entry (kernel distance, the entry's FP32 row as the query,
  * ties to the smaller id).  A query probes its `probes` nearest coarse
  * entries and starts from the `ns` nearest entries of those clusters
- * (ascending by (distance, id); ns <= probes). */
+ * (ascending by (distance, id); ns <= probes).  Both steps run on nthreads
+ * threads; every result is a per-query (or per-entry) minimum under a total
+ * order, so the thread count does not change it. */
+typedef struct {
+  const orc_index *ix;
+  const float *queries;
+  int nq;
+  const uint64_t *entries;
+  int ne, coarse, probes, ns, use_fma;
+  int *cl;            /* ne: coarse position of each entry's cluster */
+  const int *cstart;  /* coarse + 1: cluster c's entries are members[cstart[c] .. cstart[c+1]) */
+  const uint64_t *members;
+  uint64_t *starts;
+  volatile int next;
+  volatile int err;
+} twolevel_job;
+
+static void *tl_assign_worker(void *arg) {
+  twolevel_job *j = (twolevel_job *)arg;
+  for (;;) {
+    const int f = __sync_fetch_and_add(&j->next, 1);
+    if (f >= j->ne) break;
+    if (f < j->coarse) {
+      j->cl[f] = f;
+      continue;
+    }
+    uint64_t best;
+    if (orc_nearest_entry(j->ix, row(j->ix, j->entries[f]), 1, j->entries, j->coarse, 1, j->use_fma, &best) != 0) {
+      j->err = 1;
+      break;
+    }
+    int c = 0;
+    while (j->entries[c] != best) ++c; /* the coarse position of that id */
+    j->cl[f] = c;
+  }
+  return NULL;
+}
+
+static void *tl_query_worker(void *arg) {
+  twolevel_job *j = (twolevel_job *)arg;
+  uint64_t *pc = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)j->probes);
+  uint64_t *cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)j->ne);
+  if (!pc || !cand) {
+    j->err = 1;
+    free(pc);
+    free(cand);
+    return NULL;
+  }
+  for (;;) {
+    const int i = __sync_fetch_and_add(&j->next, 1);
+    if (i >= j->nq) break;
+    const float *q = j->queries + (size_t)i * (size_t)j->ix->dim;
+    if (orc_nearest_entry(j->ix, q, 1, j->entries, j->coarse, j->probes, j->use_fma, pc) != 0) {
+      j->err = 1;
+      break;
+    }
+    int nc = 0;
+    for (int p = 0; p < j->probes; ++p) {
+      int c = 0;
+      while (j->entries[c] != pc[p]) ++c;
+      for (int m = j->cstart[c]; m < j->cstart[c + 1]; ++m) cand[nc++] = j->members[m];
+    }
+    if (orc_nearest_entry(j->ix, q, 1, cand, nc, j->ns, j->use_fma, j->starts + (size_t)i * (size_t)j->ns) != 0) {
+      j->err = 1;
+      break;
+    }
+  }
+  free(pc);
+  free(cand);
+  return NULL;
+}
+
+static int tl_pool(void *(*fn)(void *), twolevel_job *j, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  int started = 0;
+  j->next = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    if (pthread_create(&th[t], NULL, fn, j) != 0) break;
+    ++started;
+  }
+  if (started == 0) fn(j);
+  for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+  return j->err ? -1 : 0;
+}
+
 int orc_nearest_entry_2level(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
-                             int coarse, int probes, int ns, int use_fma, uint64_t *starts) {
+                             int coarse, int probes, int ns, int use_fma, uint64_t *starts, int nthreads) {
   if (check_index(ix) || !queries || !entries || !starts || ne < 1 || coarse < 1 || coarse > ne || probes < 1 ||
       probes > coarse || ns < 1 || ns > probes)
     return -1;
   for (int e = 0; e < ne; ++e)
     if (entries[e] >= ix->n) return -1;
   int *cl = (int *)malloc(sizeof(int) * (size_t)ne);
-  uint64_t *pc = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)probes);
-  uint64_t *cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)ne);
-  if (!cl || !pc || !cand) {
-    free(cl);
-    free(pc);
-    free(cand);
-    return -1;
-  }
-  for (int f = 0; f < ne; ++f) {
-    if (f < coarse) {
-      cl[f] = f;
-      continue;
-    }
-    uint64_t best;
-    if (orc_nearest_entry(ix, row(ix, entries[f]), 1, entries, coarse, 1, use_fma, &best) != 0) {
-      free(cl);
-      free(pc);
-      free(cand);
-      return -1;
-    }
-    int c = 0;
-    while (entries[c] != best) ++c; /* the coarse position of that id */
-    cl[f] = c;
-  }
-  int rc = 0;
-  for (int i = 0; i < nq && rc == 0; ++i) {
-    const float *q = queries + (size_t)i * (size_t)ix->dim;
-    rc = orc_nearest_entry(ix, q, 1, entries, coarse, probes, use_fma, pc);
-    int nc = 0;
-    for (int f = 0; f < ne && rc == 0; ++f)
-      for (int p = 0; p < probes; ++p)
-        if (entries[cl[f]] == pc[p]) {
-          cand[nc++] = entries[f];
-          break;
-        }
-    if (rc == 0) rc = orc_nearest_entry(ix, q, 1, cand, nc, ns, use_fma, starts + (size_t)i * (size_t)ns);
-  }
+  int *cstart = (int *)calloc((size_t)coarse + 1, sizeof(int));
+  int *fill = (int *)calloc((size_t)coarse, sizeof(int));
+  uint64_t *members = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)ne);
+  twolevel_job j;
+  memset(&j, 0, sizeof j);
+  int rc = -1;
+  if (!cl || !cstart || !fill || !members) goto done;
+  j.ix = ix;
+  j.queries = queries;
+  j.nq = nq;
+  j.entries = entries;
+  j.ne = ne;
+  j.coarse = coarse;
+  j.probes = probes;
+  j.ns = ns;
+  j.use_fma = use_fma;
+  j.cl = cl;
+  j.starts = starts;
+  if (tl_pool(tl_assign_worker, &j, nthreads) != 0) goto done;
+  /* clusters as contiguous member lists (member order does not matter: the
+   * choice is a minimum under (distance, id)) */
+  for (int f = 0; f < ne; ++f) cstart[cl[f] + 1]++;
+  for (int c = 0; c < coarse; ++c) cstart[c + 1] += cstart[c];
+  for (int f = 0; f < ne; ++f) members[cstart[cl[f]] + fill[cl[f]]++] = entries[f];
+  j.cstart = cstart;
+  j.members = members;
+  rc = tl_pool(tl_query_worker, &j, nthreads);
+done:
   free(cl);
-  free(pc);
-  free(cand);
+  free(cstart);
+  free(fill);
+  free(members);
   return rc;
 }

@@ -113,9 +113,10 @@ int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const u
  * own cluster; every other entry joins its nearest coarse entry's cluster
  * (the entry's row as the query, ties to the smaller id).  Query i probes its
  * `probes` nearest coarse entries and gets the ns nearest entries of those
- * clusters in starts[i*ns ..] (ascending; ns <= probes <= coarse). */
+ * clusters in starts[i*ns ..] (ascending; ns <= probes <= coarse), on
+ * nthreads threads. */
 int orc_nearest_entry_2level(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
-                             int coarse, int probes, int ns, int use_fma, uint64_t *starts);
+                             int coarse, int probes, int ns, int use_fma, uint64_t *starts, int nthreads);
 
 /* One query with its decision log (at most cap events; *n_events gets the
  * number produced, which may exceed cap). */

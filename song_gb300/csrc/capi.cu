@@ -47,6 +47,7 @@ int check_search_args(const song_index *ix, int nq, int pq, int k) {
 }  // namespace song
 
 namespace {
+using song::DeviceGuard;
 using song::fail;
 using song::check_search_args;
 
@@ -57,20 +58,6 @@ using song::check_search_args;
       return fail(e_ == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "%s: %s", \
                   #call, cudaGetErrorString(e_));                                         \
   } while (0)
-
-// Makes `dev` current for the scope and restores the caller's device.
-struct DeviceGuard {
-  int prev = -1;
-  bool ok = true;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
 
 template <class T>
 int grow(T **p, size_t *cap, size_t need, uint64_t *acct) {

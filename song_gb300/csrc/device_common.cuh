@@ -1,7 +1,7 @@
 // device_common.cuh -- warp-cooperative building blocks of the search kernel:
 // bulk-copy / mbarrier wrappers (inline PTX, sm_90+ forms valid on sm_103a),
-// the visited hash and the sorted candidate / top-pq queues, all held in the
-// shared memory slice of one warp.
+// the sort keys of the candidate / top-pq queues, and the visited hashes held
+// in the shared memory slice of one warp.
 #pragma once
 
 #include <cstdint>
@@ -300,51 +300,6 @@ struct ExactVisited {
     }
     if (lane == 0) tab[h] = FH_EMPTY;
     __syncwarp();
-  }
-};
-
-// ---------------------------------------------------------------------------
-// Sorted queue in a power-of-two ring of uint64 keys: a[(head + i) & mask],
-// i in [0, n), ascending.  Used for the candidate queue (pops at the head)
-// and for the top-pq list (head fixed at 0).
-// ---------------------------------------------------------------------------
-struct SortedRing {
-  uint64_t *a;
-  int mask;
-
-  __device__ __forceinline__ uint64_t at(int head, int i) const { return a[(head + i) & mask]; }
-
-  // Number of keys < key (n <= 1024): 32 evenly spaced samples locate the
-  // stride, then one 32-wide window inside it.
-  __device__ __forceinline__ int lower_bound(int head, int n, uint64_t key, int lane) const {
-    if (n == 0) return 0;
-    int s = (n + 31) >> 5;
-    int i1 = lane * s;
-    bool lt1 = i1 < n && at(head, i1) < key;
-    int c = __popc(__ballot_sync(FULL, lt1));
-    if (c == 0) return 0;
-    int lo = (c - 1) * s + 1;
-    int hi = min(c * s, n);
-    int i2 = lo + lane;
-    bool lt2 = i2 < hi && at(head, i2) < key;
-    return lo + __popc(__ballot_sync(FULL, lt2));
-  }
-
-  // Insert at its sorted place; the keys after it move up one slot.
-  __device__ __forceinline__ void insert(int head, int &n, uint64_t key, int lane) {
-    int pos = lower_bound(head, n, key, lane);
-    for (int hi = n; hi > pos; hi -= 32) {
-      int lo = max(pos, hi - 32);
-      int i = lo + lane;
-      uint64_t v = 0;
-      if (i < hi) v = at(head, i);
-      __syncwarp();
-      if (i < hi) a[(head + i + 1) & mask] = v;
-      __syncwarp();
-    }
-    if (lane == 0) a[(head + pos) & mask] = key;
-    __syncwarp();
-    ++n;
   }
 };
 

@@ -668,8 +668,9 @@ extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int c
     if (std::adjacent_find(u.begin(), u.end()) != u.end()) return fail(SONG_ERR_ARG, "entry ids must be distinct");
   }
   if (ix->servers > 0) return fail(SONG_ERR_ARG, "entries are in use by %d server(s)", ix->servers);
-  cudaError_t e = cudaSetDevice(ix->device);
-  if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  DeviceGuard guard(ix->device);
+  if (!guard.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  cudaError_t e = cudaSuccess;
   clear_entries(ix);
   if (count == 0) return SONG_OK;
   const int dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
@@ -727,8 +728,9 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
     if (std::adjacent_find(u.begin(), u.end()) != u.end()) return fail(SONG_ERR_ARG, "entry ids must be distinct");
   }
   if (ix->servers > 0) return fail(SONG_ERR_ARG, "entries are in use by %d server(s)", ix->servers);
-  cudaError_t e = cudaSetDevice(ix->device);
-  if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  DeviceGuard guard(ix->device);
+  if (!guard.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  cudaError_t e = cudaSuccess;
   clear_entries(ix);
   // 1. all entry rows in list order; the clusters of the non-coarse entries
   uint32_t *d_ids = nullptr, *d_assign = nullptr, *d_perm = nullptr;

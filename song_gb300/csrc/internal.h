@@ -60,6 +60,20 @@ int launch_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *out, c
 struct song_index;
 
 namespace song {
+// Makes `dev` current for the scope and restores the caller's device.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
 // Error reporting of the C ABI (capi.cu): records the message for
 // song_last_error() on the calling thread and returns `code`.
 int fail(int code, const char *fmt, ...);

@@ -121,8 +121,16 @@ def recall(found, gt_ids, k):
 def recall_tie_aware(found, data, queries, kth, metric, k):
     """Fraction of the first k returned ids whose exact distance is <= the
     exact k-th nearest distance (equal distances count as correct, which
-    matters for integer-valued L2 data where ties are common)."""
+    matters for integer-valued L2 data where ties are common).  An id
+    returned twice in one row counts once: the reference's visited hash can
+    lose an entry, and the search can then list that vertex again."""
     f = np.asarray(found)[:, :k]
     d = distances_fp64(data, queries, f, metric)
     ok = d <= kth[:, None] + 1e-12 * np.abs(kth[:, None])
-    return float(ok.sum()) / float(f.shape[0] * k)
+    order = np.argsort(f, axis=1, kind="stable")
+    fs = np.take_along_axis(f, order, 1)
+    first = np.ones_like(fs, dtype=bool)
+    first[:, 1:] = fs[:, 1:] != fs[:, :-1]
+    distinct = np.empty_like(first)
+    np.put_along_axis(distinct, order, first, 1)
+    return float((ok & distinct).sum()) / float(f.shape[0] * k)

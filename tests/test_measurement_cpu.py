@@ -61,6 +61,9 @@ def test_recall_definitions():
     # an empty slot (UINT64_MAX) is never correct
     empty = np.array([[0, 0xFFFFFFFFFFFFFFFF]], dtype=np.uint64)
     assert GT.recall_tie_aware(empty, data, q, kth, "l2", 2) == 0.5
+    # an id returned twice (a vertex the visited hash lost, listed again) counts once
+    assert GT.recall_tie_aware(np.array([[0, 0]]), data, q, kth, "l2", 2) == 0.5
+    assert GT.recall_tie_aware(np.array([[1, 0, 1]]), data, q, kth, "l2", 3) == pytest.approx(2 / 3)
 
 
 @pytest.mark.parametrize("kind,lo,hi,integer", [("byte", 0, 255, True), ("unit", -1, 1, False),

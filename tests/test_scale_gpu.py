@@ -1,16 +1,25 @@
-"""The 1,000,000 x 128 L2 workload at full size, where the oracle is too slow
-to replay every query, checked through properties that hold at any size:
+"""The 1,000,000 x 128 L2 workload at full size (10,000 queries, pq 55),
+checked against the oracle query by query:
 
-* every row holds distinct valid ids, in ascending exact distance, ties in
-  ascending id.  The values are integers 0-255, so every partial sum of a
-  distance is an integer below 2^24 and the kernel's FP32 distance is the
-  exact one, whatever the summation order;
-* the first k ids of a search with k = pq are the k-id search's (one search,
-  one top list);
-* the same ids again on a second run, and through the device-buffer call;
-* from the two-level entry points (262,144 entries, 2048 clusters, 4 probed,
-  4 starts) recall@10 against the FP64 exact kNN reaches 0.95 at pq 55, and
-  the search needs fewer hops than from vertex 0 at the same pq."""
+* from vertex 0 (the reference's start) and from the two-level entry points
+  (262,144 entries, 2048 clusters, 4 probed, 4 starts), the kernel's ids,
+  hop counts and distance-evaluation counts equal the oracle's LEX mode (the
+  kernel's specification, orc_kernel_search / orc_kernel_search_from) on
+  every query, and the starts the GPU picks are the oracle's
+  orc_nearest_entry_2level choice (checked through the search they seed);
+* a row may hold an id twice: the visited hash is the reference's FixHash,
+  whose backward-shift delete can lose an entry (fixhash.h:51-93), and a
+  vertex lost from it can be queued, popped and listed again
+  (warp_astar_accelerator.h:189,202,206,313,317).  Every such row must hold
+  the same repeated id in the oracle's REF mode (the reference's own heaps
+  and hash), unless REF and LEX part at a float tie on that query;
+* size-independent properties: ids valid, exact distances non-decreasing
+  along each row (the values are integers 0-255, so every FP32 partial sum
+  is exact and the kernel's distances are the exact ones), the first k ids
+  of the k = pq search are the k-id search's, the device-buffer call gives
+  the same ids;
+* from the entry points recall@10 against the FP64 exact kNN reaches 0.95
+  at pq 55, with fewer hops than from vertex 0."""
 import os
 
 import numpy as np
@@ -19,6 +28,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 MISSING = np.uint64(0xFFFFFFFFFFFFFFFF)
+PQ = 55
 
 
 @pytest.fixture(scope="module")
@@ -30,7 +40,7 @@ def scale(song):
     graph = song.graph_build_gpu(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150, batch_div=64,
                                  device=0, nthreads=os.cpu_count())
     ix = song.Index(graph, data, w.shift, w.metric)
-    yield w, data, queries, ix
+    yield w, data, queries, graph, ix
     ix.free()
 
 
@@ -38,51 +48,88 @@ def _well_formed(ids, data, queries):
     from song_gb300 import groundtruth as GT
     n = data.shape[0]
     valid = ids != MISSING
-    # a missing slot is only ever followed by missing slots
-    assert np.all(valid[:, :-1] | ~valid[:, 1:])
+    assert np.all(valid[:, :-1] | ~valid[:, 1:])  # a missing slot is only followed by missing slots
     assert np.all(ids[valid] < n)
-    for row, v in zip(ids, valid):
-        assert len(set(row[v].tolist())) == int(v.sum())
     d = GT.distances_fp64(data, queries, ids, "l2")
     step = np.diff(d, axis=1)
-    both = valid[:, 1:]
-    assert np.all(step[both] >= 0)
-    tie = both & (step == 0)
-    assert np.all(np.diff(ids.astype(np.int64), axis=1)[tie] > 0)
+    assert np.all(step[valid[:, 1:]] >= 0)
 
 
-def test_full_scale_plain_search_properties(song, scale):
-    w, data, queries, ix = scale
-    ids10, hops, evals = ix.search(queries, 55, 10, stats=True)
-    _well_formed(ids10, data, queries)
-    full = ix.search(queries, 55, 55)
-    _well_formed(full, data, queries)
-    assert np.array_equal(full[:, :10], ids10)
-    assert np.array_equal(ix.search(queries, 55, 10), ids10)
-    assert np.all(hops > 0) and np.all(evals >= hops)
+def _repeats(ids):
+    """{row: sorted ids that occur more than once in it}."""
+    out = {}
+    for i, row in enumerate(ids):
+        r = row[row != MISSING]
+        u, c = np.unique(r, return_counts=True)
+        if np.any(c > 1):
+            out[i] = u[c > 1].tolist()
+    return out
 
 
-def test_full_scale_entry_points_reach_the_recall_target(song, scale):
+def _check_against_oracle(O, ox, gpu, queries, starts):
+    """GPU == oracle LEX on every query; returns (rows with a repeated id,
+    those whose REF row lacks the repeat, queries where REF and LEX differ)."""
+    ids, hops, evals = gpu
+    if starts is None:
+        o_ids, o_hops, o_evals, _ = ox.kernel_search(queries, PQ, O.MODE_LEX)
+        r_ids = ox.kernel_search(queries, PQ, O.MODE_REF)[0]
+    else:
+        o_ids, o_hops, o_evals, _ = ox.kernel_search_from(queries, starts, PQ, O.MODE_LEX)
+        r_ids = ox.kernel_search_from(queries, starts, PQ, O.MODE_REF)[0]
+    bad = np.nonzero(~np.all(ids == o_ids, axis=1) | (hops != o_hops) | (evals != o_evals))[0]
+    assert bad.size == 0, "queries differing from oracle LEX: %s" % bad[:20].tolist()
+    rep = _repeats(ids)
+    not_in_ref = [i for i, dup in rep.items() if not set(dup) <= set(_repeats(r_ids[i:i + 1]).get(0, []))]
+    differ = np.nonzero(~np.all(r_ids == o_ids, axis=1))[0]
+    # a REF row without the repeat is allowed only where REF and LEX part
+    assert set(not_in_ref) <= set(differ.tolist()), not_in_ref
+    return rep, not_in_ref, differ
+
+
+def test_full_scale_vertex0_equals_oracle(song, oracle, scale):
+    w, data, queries, graph, ix = scale
+    ids, hops, evals = ix.search(queries, PQ, PQ, stats=True)
+    _well_formed(ids, data, queries)
+    ox = oracle.OracleIndex(data, graph, w.shift, oracle.METRICS[w.metric])
+    rep, not_in_ref, differ = _check_against_oracle(oracle, ox, (ids, hops, evals), queries, None)
+    print("vertex 0, pq %d: %d rows with a repeated id (FixHash lost entries): %s; REF differs from LEX on %d "
+          "queries" % (PQ, len(rep), sorted(rep)[:10], differ.size))
+    # where REF and LEX part, their decision logs first differ at a float tie
+    for i in differ[:50]:
+        _, la = ox.kernel_search_log(queries[i], PQ, oracle.MODE_REF)
+        _, lb = ox.kernel_search_log(queries[i], PQ, oracle.MODE_LEX)
+        assert oracle.classify(la, lb)[0] == 1, i
+    ids10 = ix.search(queries, PQ, 10)
+    assert np.array_equal(ids[:, :10], ids10)
+    assert np.array_equal(ix.search(queries, PQ, 10), ids10)
+
+
+def test_full_scale_entry_points_equal_oracle_and_reach_the_recall_target(song, oracle, scale):
     import torch
     from song_gb300 import datasets as D
     from song_gb300 import groundtruth as GT
-    w, data, queries, ix = scale
-    _, plain_hops, _ = ix.search(queries, 55, 10, stats=True)
-    ix.set_entries(song.sample_entries(w.n, 262144, seed=D.SEED_BASE + 10, shuffle=True), starts=4, coarse=2048,
-                   probes=4)
+    w, data, queries, graph, ix = scale
+    _, plain_hops, _ = ix.search(queries, PQ, 10, stats=True)
+    ent = song.sample_entries(w.n, 262144, seed=D.SEED_BASE + 10, shuffle=True)
+    ix.set_entries(ent, starts=4, coarse=2048, probes=4)
     try:
-        ids, hops, evals = ix.search(queries, 55, 10, stats=True)
+        ids, hops, evals = ix.search(queries, PQ, PQ, stats=True)
         _well_formed(ids, data, queries)
+        ox = oracle.OracleIndex(data, graph, w.shift, oracle.METRICS[w.metric])
+        starts = ox.nearest_entry_2level(queries, ent, 2048, 4, 4)
+        rep, not_in_ref, differ = _check_against_oracle(oracle, ox, (ids, hops, evals), queries, starts)
+        print("entry points, pq %d: %d rows with a repeated id: %s; REF differs from LEX on %d queries"
+              % (PQ, len(rep), sorted(rep)[:10], differ.size))
         # the device-buffer call on a stream gives the same ids
         dq = torch.from_numpy(np.ascontiguousarray(queries)).cuda()
         out = torch.empty((queries.shape[0], 10), dtype=torch.int64, device="cuda")
         stream = torch.cuda.Stream()
         torch.cuda.synchronize()  # the upload above ran on another stream
-        ix.search_device(dq.data_ptr(), queries.shape[0], 55, 10, out.data_ptr(), None, None, stream.cuda_stream)
+        ix.search_device(dq.data_ptr(), queries.shape[0], PQ, 10, out.data_ptr(), None, None, stream.cuda_stream)
         stream.synchronize()
-        assert np.array_equal(out.cpu().numpy().view(np.uint64), ids)
+        assert np.array_equal(out.cpu().numpy().view(np.uint64), ids[:, :10])
         _, kth = GT.exact_knn_fp64(data, queries, 10, "l2")
-        rec = GT.recall_tie_aware(ids, data, queries, kth, "l2", 10)
+        rec = GT.recall_tie_aware(ids[:, :10], data, queries, kth, "l2", 10)
         assert rec >= 0.95, rec
         assert hops.mean() < plain_hops.mean()
     finally:
