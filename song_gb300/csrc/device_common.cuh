@@ -139,9 +139,10 @@ struct VisitedHash {
   }
 
   // Whole warp, one key (fixhash.h:38-47): first EMPTY/DELETION slot on the
-  // probe sequence, found 32 slots at a time with a ballot.
-  __device__ __forceinline__ void add(uint32_t id, int lane) {
-    int base = slot(id);
+  // probe sequence, found 32 slots at a time with a ballot.  `home` is
+  // slot(id), computed by the caller (often in parallel, one lane per key).
+  __device__ __forceinline__ void add_at(uint32_t id, int home, int lane) {
+    int base = home;
     for (int w = 0; w * 32 < cap + 32; ++w) {
       int s = wrap(base + lane);
       int32_t v = tab[s];
@@ -155,13 +156,16 @@ struct VisitedHash {
     __syncwarp();
   }
 
-  // Whole warp, one key (fixhash.h:59-93).  The run after the removed entry is
-  // read 32 slots at a time; the reference's sequential case analysis then
-  // runs uniformly over it, with each lane's slot value and home slot fetched
-  // by shuffle.
-  __device__ __forceinline__ void del(uint32_t id, int lane) {
+  __device__ __forceinline__ void add(uint32_t id, int lane) { add_at(id, slot(id), lane); }
+
+  // Whole warp, one key (fixhash.h:59-93), `home` = slot(id).  The run after
+  // the removed entry is read 32 slots at a time; the reference's sequential
+  // case analysis then runs uniformly over it, with each lane's slot value
+  // and home slot fetched by shuffle.  Home slots of the run are computed
+  // only when the slot after the removed entry is occupied.
+  __device__ __forceinline__ void del_at(uint32_t id, int home, int lane) {
     const int32_t x = static_cast<int32_t>(id);
-    int code = slot(id);
+    int code = home;
     int r = -1;
     int base = code;
     for (int w = 0; w * 32 < cap + 32; ++w) {
@@ -183,12 +187,13 @@ struct VisitedHash {
     for (int w = 0; w * 32 < cap + 32; ++w) {
       int s = wrap(nbase + lane);
       int32_t v = tab[s];
-      int home = v >= 0 ? slot(static_cast<uint32_t>(v)) : 0;
       unsigned be = __ballot_sync(FULL, v == FH_EMPTY);
       int run = be ? __ffs(be) - 1 : 32;
+      int hv = 0;
+      if (run > 0) hv = v >= 0 ? slot(static_cast<uint32_t>(v)) : 0;  // warp-uniform branch
       for (int i = 0; i < run; ++i) {
         int nxt = wrap(nbase + i);
-        int ncode = __shfl_sync(FULL, home, i);
+        int ncode = __shfl_sync(FULL, hv, i);
         int32_t val = __shfl_sync(FULL, v, i);
         bool cond1 = code <= r;
         bool cond2 = r < nxt;
@@ -209,6 +214,8 @@ struct VisitedHash {
     if (lane == 0) tab[r] = FH_EMPTY;
     __syncwarp();
   }
+
+  __device__ __forceinline__ void del(uint32_t id, int lane) { del_at(id, slot(id), lane); }
 };
 
 // ---------------------------------------------------------------------------
@@ -245,8 +252,8 @@ struct ExactVisited {
     return false;
   }
 
-  __device__ __forceinline__ void add(uint32_t id, int lane) {
-    int base = slot(id);
+  __device__ __forceinline__ void add_at(uint32_t id, int home, int lane) {
+    int base = home;
     for (int w = 0; w * 32 < cap + 32; ++w) {
       const int s = wrap(base + lane);
       const int32_t v = tab[s];
@@ -260,9 +267,11 @@ struct ExactVisited {
     __syncwarp();
   }
 
-  __device__ __forceinline__ void del(uint32_t id, int lane) {
+  __device__ __forceinline__ void add(uint32_t id, int lane) { add_at(id, slot(id), lane); }
+
+  __device__ __forceinline__ void del_at(uint32_t id, int home, int lane) {
     const int32_t x = static_cast<int32_t>(id);
-    int base = slot(id), h = -1;
+    int base = home, h = -1;
     for (int w = 0; w * 32 < cap + 32; ++w) {
       const int s = wrap(base + lane);
       const int32_t v = tab[s];
@@ -301,6 +310,8 @@ struct ExactVisited {
     if (lane == 0) tab[h] = FH_EMPTY;
     __syncwarp();
   }
+
+  __device__ __forceinline__ void del(uint32_t id, int lane) { del_at(id, slot(id), lane); }
 };
 
 }  // namespace song

@@ -120,8 +120,58 @@ __device__ __forceinline__ float load_elem(const uint8_t *row, int j, float scal
   return __fmul_rn(__half2float(__half(h)), scale);
 }
 
+// Two FP32 lanes in one 64-bit register, for the paired FP32 instructions of
+// sm_100-family GPUs (sub/fma .rn.f32x2: each half rounded to nearest even,
+// exactly the scalar __fsub_rn / __fmaf_rn).
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t r, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// The xor butterfly 16, 8, 4, 2, 1 over the 32 lanes' partial sums of H rows
+// at once.  At the first log2(H) levels each lane keeps half of its rows and
+// sends its partner the other half, so one shuffle serves two rows; every
+// row still meets its partials in the butterfly's pairs (each pair sum is
+// the same two floats, and a + b == b + a), so the sums are bit for bit the
+// per-row butterfly's.  Returns, in lane l, the sum of row l / (32 / H).
+template <int H>
+__device__ __forceinline__ float butterfly_rows(float (&v)[H], int lane) {
+  static_assert(H >= 1 && H <= 32 && (H & (H - 1)) == 0, "H must be a power of two");
+  int o = 16;
+#pragma unroll
+  for (int n = H; n > 1; n >>= 1, o >>= 1) {
+    const bool hi = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < n / 2; ++i) {
+      const float keep = hi ? v[i + n / 2] : v[i];
+      const float send = hi ? v[i] : v[i + n / 2];
+      v[i] = __fadd_rn(keep, __shfl_xor_sync(FULL, send, o));
+    }
+  }
+#pragma unroll
+  for (; o > 0; o >>= 1) v[0] = __fadd_rn(v[0], __shfl_xor_sync(FULL, v[0], o));
+  return v[0];
+}
+
 // Distances of candidates 0..m-1 (candidate c's id in lane c); candidate c's
 // distance is returned in lane c.  False if a bulk copy never completed.
+// Rows are taken in pairs through the paired FP32 instructions (the same
+// roundings, in the same order, as the scalar form: lane l sums dims l, l+32,
+// ... of each row with fused multiply-add).
 template <int METRIC, int STORAGE, int H>
 __device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage, uint64_t *mbar,
                                                  uint32_t &ph0, uint32_t &ph1, const float *qv,
@@ -154,37 +204,64 @@ __device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage
     const int cnt = min(H, m - first);
     const uint8_t *buf = stage + static_cast<size_t>(b * H) * rb;
     float acc[H], len[H];
+    if constexpr (H == 1) {
+      float a = 0.0f, l2 = 0.0f;
+      const float scale = STORAGE == 2 ? *reinterpret_cast<const float *>(buf + p.scale_off) : 1.0f;
+      for (int j = lane; j < p.dim; j += 32) {
+        const float qj = qv[j];
+        const float xj = load_elem<STORAGE>(buf, j, scale);
+        if (METRIC == 0) {
+          const float d = __fsub_rn(qj, xj);
+          a = __fmaf_rn(d, d, a);
+        } else {
+          a = __fmaf_rn(qj, xj, a);
+          if (METRIC == 2) l2 = __fmaf_rn(xj, xj, l2);
+        }
+      }
+      acc[0] = a;
+      len[0] = l2;
+    } else {
+      constexpr int P = H / 2;  // row pairs
+      uint64_t a2[P], l2[P];
+      float sc[H];
 #pragma unroll
-    for (int i = 0; i < H; ++i) {
-      acc[i] = 0.0f;
-      len[i] = 0.0f;
-      if (i < cnt) {
-        const uint8_t *x = buf + static_cast<size_t>(i) * rb;
-        const float scale = STORAGE == 2 ? *reinterpret_cast<const float *>(x + p.scale_off) : 1.0f;
-        for (int j = lane; j < p.dim; j += 32) {
-          const float qj = qv[j];
-          const float xj = load_elem<STORAGE>(x, j, scale);
-          if (METRIC == 0) {
-            const float d = __fsub_rn(qj, xj);
-            acc[i] = __fmaf_rn(d, d, acc[i]);
-          } else {
-            acc[i] = __fmaf_rn(qj, xj, acc[i]);
-            if (METRIC == 2) len[i] = __fmaf_rn(xj, xj, len[i]);
+      for (int i = 0; i < P; ++i) a2[i] = l2[i] = 0ull;
+#pragma unroll
+      for (int i = 0; i < H; ++i)
+        sc[i] = STORAGE == 2 ? *reinterpret_cast<const float *>(buf + static_cast<size_t>(i) * rb + p.scale_off) : 1.0f;
+#pragma unroll 2
+      for (int j = lane; j < p.dim; j += 32) {
+        const float qj = qv[j];
+        const uint64_t qq = f2_pack(qj, qj);
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+          if (2 * i < cnt) {  // warp-uniform
+            const float x0 = load_elem<STORAGE>(buf + static_cast<size_t>(2 * i) * rb, j, sc[2 * i]);
+            const float x1 = load_elem<STORAGE>(buf + static_cast<size_t>(2 * i + 1) * rb, j, sc[2 * i + 1]);
+            const uint64_t xx = f2_pack(x0, x1);
+            if (METRIC == 0) {
+              const uint64_t d = f2_sub(qq, xx);
+              a2[i] = f2_fma(d, d, a2[i]);
+            } else {
+              a2[i] = f2_fma(qq, xx, a2[i]);
+              if (METRIC == 2) l2[i] = f2_fma(xx, xx, l2[i]);
+            }
           }
         }
       }
-    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-      for (int i = 0; i < H; ++i) {
-        acc[i] = __fadd_rn(acc[i], __shfl_xor_sync(FULL, acc[i], o));
-        if (METRIC == 2) len[i] = __fadd_rn(len[i], __shfl_xor_sync(FULL, len[i], o));
+      for (int i = 0; i < P; ++i) {
+        f2_unpack(a2[i], acc[2 * i], acc[2 * i + 1]);
+        f2_unpack(l2[i], len[2 * i], len[2 * i + 1]);
       }
     }
-#pragma unroll
-    for (int i = 0; i < H; ++i)
-      if (i < cnt && lane == first + i) out = finish_distance<METRIC>(acc[i], len[i]);
+    // Row r's sums are in lanes r*(32/H) .. ; candidate first + i takes row i.
+    const float t = butterfly_rows<H>(acc, lane);
+    const float ln = METRIC == 2 ? butterfly_rows<H>(len, lane) : 0.0f;
+    const int src = ((lane - first) & (H - 1)) * (32 / H);
+    const float ts = __shfl_sync(FULL, t, src);
+    const float ls = METRIC == 2 ? __shfl_sync(FULL, ln, src) : 0.0f;
+    if (lane >= first && lane < first + cnt) out = finish_distance<METRIC>(ts, ls);
     __syncwarp();
     if (c + 2 < nchunks) issue(c + 2);
   }
@@ -367,7 +444,8 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
     uint32_t a = a_next;
     if (now_id != next_id)  // not taken: the prefetch predicts the pop exactly
       a = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(now_id) << p.shift) + lane) : 0u;
-    vh.del(now_id, lane);
+    const int now_home = vh.slot(now_id);
+    vh.del_at(now_id, now_home, lane);
     // :191 finish test (<=) against the list maximum.
     if (tn == pq && key_dist(T.max()) <= key_dist(now)) break;
     ++hops;
@@ -383,7 +461,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
     {
       const uint64_t ev = T.max();
       T.insert_evict(now, lane);
-      vh.add(now_id, lane);
+      vh.add_at(now_id, now_home, lane);
       if (tn < pq) ++tn;
       else vh.del(key_id(ev), lane);
     }
@@ -412,21 +490,39 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
       next_id = key_id(nk);
       a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
     }
-    // :297-322 select-insert in candidate order.
+    // :297-322 select-insert in candidate order, in two passes.  The queue
+    // pass applies the select-insert rule and the insertions and notes, in
+    // lane c, the key candidate c's insertion pushed out (~0: none, the
+    // queue was not full).  Below pq live keys the window's maximum is an
+    // infinite key, which leaves and is never below a candidate; at pq, the
+    // select-insert rule, then the larger of the key and the maximum leaves
+    // (:315-320).  The hash pass then makes the reference's visited-hash
+    // calls in the reference's order -- add(candidate), delete(pushed-out
+    // key) per inserted candidate -- with every home slot computed up front,
+    // one lane per key.  (Queue and hash are independent, so splitting the
+    // passes changes neither.)
+    const int chome = vh.slot(cid);
+    uint64_t my_ev = ~0ull;
+    unsigned ins = 0u;
     for (int c = 0; c < m; ++c) {
-      const float d = __shfl_sync(FULL, cd, c);
-      const uint32_t id = __shfl_sync(FULL, cid, c);
-      const uint64_t key = make_key(d, id);
-      // Below pq live keys the window's maximum is an infinite key, which
-      // leaves; at pq, the select-insert rule, then the larger of the key
-      // and the maximum leaves (:315-320).
+      const uint64_t key = __shfl_sync(FULL, ck, c);
       const uint64_t qmax = Q.max();
-      if (qn >= pq && key_dist(qmax) < key_dist(key)) continue;
+      if (key_dist(qmax) < key_dist(key)) continue;
       const uint64_t ev = key < qmax ? qmax : key;
       Q.insert_evict(key, lane);
-      vh.add(id, lane);
+      ins |= 1u << c;
+      if (lane == c) my_ev = ev;
       if (qn < pq) ++qn;
-      else vh.del(key_id(ev), lane);
+    }
+    if (ins) {
+      const int ehome = my_ev != ~0ull ? vh.slot(key_id(my_ev)) : 0;
+      do {
+        const int c = __ffs(ins) - 1;
+        ins &= ins - 1u;
+        vh.add_at(__shfl_sync(FULL, cid, c), __shfl_sync(FULL, chome, c), lane);
+        const uint64_t ev = __shfl_sync(FULL, my_ev, c);
+        if (ev != ~0ull) vh.del_at(key_id(ev), __shfl_sync(FULL, ehome, c), lane);
+      } while (ins);
     }
     if (LEARNED) {
       const bool check = p.mlp && hops >= p.exit_min_hops && (hops % p.exit_every) == 0 && tn >= k;
