@@ -26,7 +26,7 @@ CUDA_SOURCES = ["search.cu", "search_f32.cu", "search_bf16.cu", "search_fp8.cu",
                 "capi.cu", "noalloc.cu", "mlp.cu", "serve.cu", "graph_build_gpu.cu", "entries.cu"]
 CXX_SOURCES = ["graph_build.cpp"]
 HEADERS = ["device_common.cuh", "internal.h", "reg_queue.cuh", "search_kernel.cuh", "graph_build.h",
-           "entry_choice.cuh"]
+           "entry_choice.cuh", "entry_tiles.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -90,6 +90,8 @@ void release(song_index *ix) {
   cudaFree(ix->d_entry_rows);
   cudaFree(ix->d_coarse_rows);
   cudaFree(ix->d_offsets);
+  cudaFree(ix->d_cl_count);
+  cudaFree(ix->d_entry_work);
   cudaFree(ix->d_starts);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;

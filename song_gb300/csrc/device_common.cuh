@@ -71,6 +71,58 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   return false;
 }
 
+// Two FP32 lanes in one 64-bit register, for the paired FP32 instructions of
+// sm_100-family GPUs (sub/fma .rn.f32x2: each half rounded to nearest even,
+// exactly the scalar __fsub_rn / __fmaf_rn).
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t r, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
+// The xor butterfly 16, 8, 4, 2, 1 over the 32 lanes' partial sums of H rows
+// at once.  At the first log2(H) levels each lane keeps half of its rows and
+// sends its partner the other half, so one shuffle serves two rows; every
+// row still meets its partials in the butterfly's pairs (each pair sum is
+// the same two floats, and a + b == b + a), so the sums are bit for bit the
+// per-row butterfly's.  Returns, in lane l, the sum of row l / (32 / H).
+template <int H>
+__device__ __forceinline__ float butterfly_rows(float (&v)[H], int lane) {
+  static_assert(H >= 1 && H <= 32 && (H & (H - 1)) == 0, "H must be a power of two");
+  int o = 16;
+#pragma unroll
+  for (int n = H; n > 1; n >>= 1, o >>= 1) {
+    const bool hi = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < n / 2; ++i) {
+      const float keep = hi ? v[i + n / 2] : v[i];
+      const float send = hi ? v[i] : v[i + n / 2];
+      v[i] = __fadd_rn(keep, __shfl_xor_sync(FULL, send, o));
+    }
+  }
+#pragma unroll
+  for (; o > 0; o >>= 1) v[0] = __fadd_rn(v[0], __shfl_xor_sync(FULL, v[0], o));
+  return v[0];
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

@@ -14,9 +14,9 @@
 // to the partial of its lane in dimension order, and then adds them in the
 // butterfly's pairs, which gives every lane's (identical) result.  The entry
 // rows are copied once into a contiguous block, which stays in L2.  The
-// cluster phase of the two-level choice instead spreads each row over the
-// warp as the search does and adds the partials in a transposed butterfly
-// (warp_rows_distance): the same sums, read with coalesced loads.
+// two-level choice instead spreads each row over a warp as the search does,
+// 32 (query, row) pairs at a time, and adds the partials in a transposed
+// butterfly (entry_tiles.cuh): the same sums.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "entry_choice.cuh"
+#include "entry_tiles.cuh"
 #include "internal.h"
 #include "song_gb300.h"
 
@@ -362,84 +363,12 @@ cudaError_t launch_nearest(const float *queries, int nq, int qstride, int dim, i
 
 // ---------------------------------------------------------------------------
 // Two-level choice: the probes nearest coarse entries, then the ns nearest
-// entries of their clusters.
+// entries of their clusters.  Both phases score warp tiles of 4 queries x 8
+// rows (entry_tiles.cuh: exact search distances) from shared memory.  The
+// second phase runs cluster by cluster: the probe lists are inverted into one
+// query list per cluster, and a block loads each cluster's rows once for all
+// queries probing it.  Each query's per-cluster best lists are then merged.
 // ---------------------------------------------------------------------------
-
-// The search distances of rows base .. base+nr-1 (nr <= 32) to the staged
-// query qw (dpad floats), computed by the whole warp; lane l returns row
-// base+l's.  Lane l reads dimensions l, l+32, ... of every row, so each read
-// is one coalesced line per row, and keeps the FMA partial sum of those
-// dimensions, which is partial l of entry_distance.  A transposed xor
-// butterfly then adds the 32 rows' partials in the butterfly's pairs: at the
-// step with offset o a lane keeps the half of its rows selected by bit o of
-// its lane number and adds the partner's partials of that half, so after the
-// last step lane l holds row l's sum, bit for bit entry_distance's.
-template <int METRIC>
-__device__ __forceinline__ float warp_rows_distance(const float *rows, int dpad, uint32_t base, int nr,
-                                                    const float *qw, int lane) {
-  constexpr int U = 4;  // rows whose loads are issued together
-  float t[32], l[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) t[i] = l[i] = 0.0f;
-#pragma unroll
-  for (int u0 = 0; u0 < 32; u0 += U) {
-    if (u0 < nr) {
-      const float *r0 = rows + static_cast<size_t>(base + u0) * dpad;
-      for (int j = 0; 32 * j < dpad; j += 4) {
-        float qv[4], x[U][4];
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const int d = lane + 32 * (j + jj);
-          qv[jj] = d < dpad ? qw[d] : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-#pragma unroll
-          for (int jj = 0; jj < 4; ++jj) {
-            const int d = lane + 32 * (j + jj);
-            x[u][jj] = (u0 + u < nr && d < dpad) ? __ldg(r0 + static_cast<size_t>(u) * dpad + d) : 0.0f;
-          }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-#pragma unroll
-          for (int jj = 0; jj < 4; ++jj) {
-            const int d = lane + 32 * (j + jj);
-            if (u0 + u < nr && d < dpad) {
-              if (METRIC == SONG_METRIC_L2) {
-                const float df = __fsub_rn(qv[jj], x[u][jj]);
-                t[u0 + u] = __fmaf_rn(df, df, t[u0 + u]);
-              } else {
-                t[u0 + u] = __fmaf_rn(qv[jj], x[u][jj], t[u0 + u]);
-                if (METRIC == SONG_METRIC_COS) l[u0 + u] = __fmaf_rn(x[u][jj], x[u][jj], l[u0 + u]);
-              }
-            }
-          }
-      }
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int i = 0; i < o; ++i) {
-      const float ts = up ? t[i] : t[i + o];
-      const float tk = up ? t[i + o] : t[i];
-      t[i] = __fadd_rn(tk, __shfl_xor_sync(0xffffffffu, ts, o));
-      if (METRIC == SONG_METRIC_COS) {
-        const float ls = up ? l[i] : l[i + o];
-        const float lk = up ? l[i + o] : l[i];
-        l[i] = __fadd_rn(lk, __shfl_xor_sync(0xffffffffu, ls, o));
-      }
-    }
-  }
-  if (METRIC == SONG_METRIC_L2) return t[0];
-  if (METRIC == SONG_METRIC_IP) return -t[0];
-  if (l[0] != 0.0f) {
-    const float sign = t[0] < 0.0f ? 1.0f : -1.0f;
-    return __fdiv_rn(__fmul_rn(__fmul_rn(sign, t[0]), t[0]), l[0]);
-  }
-  return 0.0f;
-}
 
 // 16-byte global-to-shared copies that complete without holding registers
 // (cp.async, waited for by group).
@@ -453,25 +382,72 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Two-level choice, first kernel: every query's `probes` nearest coarse
-// entries.  One warp per query; the block streams the coarse rows (sorted by
-// id, so the position is the tie order) through shared-memory tiles of 32
-// rows, lane e scoring row e of the tile.  With nbuf == 2 the next tile's
-// copies are in flight while the current tile is scored.
+constexpr int TB_WARPS = 8;                  // warps per block
+constexpr int TB_QUERIES = 4 * TB_WARPS;     // queries per block: 4 per warp
+constexpr int TB_ROWS = 32;                  // rows per staged tile: 4 groups of 8
+
+// Shared memory of a block: the staged queries, then nbuf row tiles.
+size_t tiled_smem(int dpad, int nbuf) {
+  return sizeof(float) * static_cast<size_t>(dpad) * (TB_QUERIES + static_cast<size_t>(nbuf) * TB_ROWS);
+}
+
+// Streams rows [r0, r1) of the row-major block `rows` (dpad floats each)
+// through nbuf shared-memory tiles of TB_ROWS rows (the next tile's copies in
+// flight while the current one is scored) and calls score(first_row, n, tile)
+// for each; every thread of the block takes part.  Only rows below r1 are
+// copied.
+template <class F>
+__device__ __forceinline__ void stream_rows(const float *rows, int dpad, int r0, int r1, int nbuf, float *xb,
+                                            F &&score) {
+  const size_t tile = static_cast<size_t>(dpad) * TB_ROWS;
+  auto issue = [&](int first, float *buf) {
+    const int n = min(TB_ROWS, r1 - first);
+    const float4 *src = reinterpret_cast<const float4 *>(rows + static_cast<size_t>(first) * dpad);
+    float4 *dst = reinterpret_cast<float4 *>(buf);
+    const int n4 = n * (dpad / 4);
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) cp_async16(dst + i, src + i);
+    cp_async_commit();
+  };
+  if (nbuf == 2 && r0 < r1) issue(r0, xb);
+  for (int first = r0, k = 0; first < r1; first += TB_ROWS, ++k) {
+    float *cur = xb + (nbuf == 2 ? static_cast<size_t>(k & 1) * tile : 0);
+    if (nbuf == 2) {
+      // the other buffer was last read before the previous iteration's closing barrier
+      if (first + TB_ROWS < r1) {
+        issue(first + TB_ROWS, xb + static_cast<size_t>((k + 1) & 1) * tile);
+      } else {
+        cp_async_commit();
+      }
+      cp_async_wait<1>();
+    } else {
+      issue(first, cur);
+      cp_async_wait<0>();
+    }
+    __syncthreads();  // every thread's copies (and the staged queries) are visible
+    score(first, min(TB_ROWS, r1 - first), cur);
+    __syncthreads();
+  }
+}
+
+// Two-level choice, first kernel: each query's `probes` nearest coarse
+// entries (positions in the coarse list, which is sorted by id, so the
+// position is the tie order), and the number of probes of each cluster.
+// A block takes 32 queries (4 per warp) and streams all coarse rows; lane l
+// of a warp scores its query l >> 3 against rows l & 7 of each group of 8.
 template <int METRIC, int NP>
-__global__ void __launch_bounds__(256) nearest_head_kernel(const float *queries, int nq, int dim, int dpad,
-                                                           const float *coarse_rows, int n_coarse, int probes,
-                                                           int nbuf, uint32_t *probe_out) {
-  extern __shared__ float4 sm4[];
-  constexpr int TILE = 32;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int qi = blockIdx.x * nwarps + wib;
-  const bool active = qi < nq;
-  const int d4 = dpad >> 2, rs4 = d4 + 1, tile_elems = TILE * rs4;
-  float *qw = reinterpret_cast<float *>(sm4 + nbuf * tile_elems) + static_cast<size_t>(wib) * dpad;
-  for (int j = lane; j < dpad; j += 32) qw[j] = (active && j < dim) ? queries[static_cast<size_t>(qi) * dim + j] : 0.0f;
-  const float4 *q4 = reinterpret_cast<const float4 *>(qw);
-  const float4 *src4 = reinterpret_cast<const float4 *>(coarse_rows);
+__global__ void __launch_bounds__(TB_WARPS * 32) heads_tiled_kernel(const float *queries, int nq, int dim, int dpad,
+                                                                    const float *coarse_rows, int n_coarse,
+                                                                    int probes, int nbuf, uint32_t *probe_out,
+                                                                    uint32_t *cl_count) {
+  extern __shared__ __align__(16) float smt[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int q0 = blockIdx.x * TB_QUERIES;
+  float *qs = smt;
+  float *xb = smt + static_cast<size_t>(dpad) * TB_QUERIES;
+  for (int i = threadIdx.x; i < TB_QUERIES * dpad; i += blockDim.x) {
+    const int r = i / dpad, j = i - r * dpad;
+    qs[i] = (q0 + r < nq && j < dim) ? queries[static_cast<size_t>(q0 + r) * dim + j] : 0.0f;
+  }
   float pd[NP];
   uint32_t pi[NP];
 #pragma unroll
@@ -479,124 +455,234 @@ __global__ void __launch_bounds__(256) nearest_head_kernel(const float *queries,
     pd[m] = __int_as_float(0x7f800000);
     pi[m] = 0xffffffffu;
   }
-  auto issue = [&](int t0, float4 *buf) {
-    const int rows = min(TILE, n_coarse - t0);
-    for (int i = threadIdx.x; i < rows * d4; i += blockDim.x) {
-      const int r = i / d4, c = i - r * d4;
-      cp_async16(buf + r * rs4 + c, src4 + static_cast<size_t>(t0 + r) * d4 + c);
+  const float *qw = qs + static_cast<size_t>(4 * warp) * dpad;
+  stream_rows(coarse_rows, dpad, 0, n_coarse, nbuf, xb, [&](int first, int n, const float *cur) {
+    for (int g = 0; g < n; g += 8) {
+      const float d = warp_tile_distance<METRIC>(qw, dpad, cur + static_cast<size_t>(g) * dpad, dpad, dpad, lane);
+      const int r = g + (lane & 7);
+      if (r < n) list_insert<NP>(pd, pi, d, static_cast<uint32_t>(first + r));
     }
-    cp_async_commit();
-  };
-  if (nbuf == 2) issue(0, sm4);
-  for (int t0 = 0, k = 0; t0 < n_coarse; t0 += TILE, ++k) {
-    float4 *cur = sm4 + (nbuf == 2 ? (k & 1) * tile_elems : 0);
-    if (nbuf == 2) {
-      // the other buffer was last read before the previous iteration's closing barrier
-      if (t0 + TILE < n_coarse) {
-        issue(t0 + TILE, sm4 + ((k + 1) & 1) * tile_elems);
-      } else {
-        cp_async_commit();
-      }
-      cp_async_wait<1>();  // this thread's copies of the current tile have landed
-    } else {
-      issue(t0, cur);
-      cp_async_wait<0>();
-    }
-    __syncthreads();  // ... and every thread's, as has the staged query
-    const int rows = min(TILE, n_coarse - t0);
-    if (active && lane < rows)
-      list_insert<NP>(pd, pi, entry_distance<METRIC, false>(cur + lane * rs4, q4, d4), static_cast<uint32_t>(t0 + lane));
-    __syncthreads();
-  }
-  if (!active) return;
+  });
+  const int q = q0 + 4 * warp + (lane >> 3);
   int h = 0;
   for (int r = 0; r < probes; ++r) {
-    const uint32_t c = list_take<NP>(pd, pi, h);
-    if (lane == 0) probe_out[static_cast<size_t>(qi) * probes + r] = c;
+    float wd;
+    uint32_t wid;
+    group8_take<NP>(pd, pi, h, wd, wid);
+    if ((lane & 7) == 0 && q < nq) {
+      probe_out[static_cast<size_t>(q) * probes + r] = wid;
+      atomicAdd(cl_count + wid, 1u);
+    }
   }
 }
 
-// Two-level choice, second kernel: the ns nearest entries of each query's
-// probed clusters (cluster-ordered block in L2), 32 rows at a time with
-// warp_rows_distance.  Warps are independent (no barrier), so blocks are
-// small and a query with large clusters holds only its own warp's slot.
-template <int METRIC, int NS>
-__global__ void __launch_bounds__(64, METRIC == SONG_METRIC_L2 && NS <= 4 ? 12 : 8)
-    nearest_in_clusters_kernel(const float *queries, int nq, int dim, int dpad, const float *fine_rows,
-                               const uint32_t *fine_ids, const uint32_t *offsets, const uint32_t *probe_in,
-                               int probes, int ns, uint32_t *starts) {
-  extern __shared__ float qs[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int qi = blockIdx.x * (blockDim.x >> 5) + wib;
-  if (qi >= nq) return;  // whole warps leave together
-  float *qw = qs + static_cast<size_t>(wib) * dpad;
-  for (int j = lane; j < dpad; j += 32) qw[j] = j < dim ? queries[static_cast<size_t>(qi) * dim + j] : 0.0f;
-  __syncwarp();
-  float bd[NS];
-  uint32_t bi[NS];
+// Exclusive scan of the per-cluster probe counts (one block): offs[0..n],
+// and a copy of offs[0..n-1] as the scatter cursors.
+__global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *count, int n, uint32_t *offs,
+                                                            uint32_t *cursor) {
+  __shared__ uint32_t warp_sum[32];
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t s = 0;
+  for (int i = b; i < e; ++i) s += count[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = s;  // inclusive scan within the warp
 #pragma unroll
-  for (int m = 0; m < NS; ++m) {
-    bd[m] = __int_as_float(0x7f800000);
-    bi[m] = 0xffffffffu;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  for (int r = 0; r < probes; ++r) {
-    const uint32_t c = probe_in[static_cast<size_t>(qi) * probes + r];
-    const uint32_t end = offsets[c + 1];
-    for (uint32_t b = offsets[c]; b < end; b += 32) {
-      const int nr = static_cast<int>(min(32u, end - b));
-      const float d = warp_rows_distance<METRIC>(fine_rows, dpad, b, nr, qw, lane);
-      if (lane < nr) list_insert<NS>(bd, bi, d, fine_ids[b + lane]);
+  if (lane == 31) warp_sum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < static_cast<int>(blockDim.x >> 5) ? warp_sum[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
     }
+    warp_sum[lane] = w;
   }
-  int h = 0;
-  for (int r = 0; r < ns; ++r) {
-    const uint32_t id = list_take<NS>(bd, bi, h);
-    if (lane == 0) starts[static_cast<size_t>(qi) * ns + r] = id;
+  __syncthreads();
+  uint32_t run = x - s + (warp > 0 ? warp_sum[warp - 1] : 0u);
+  for (int i = b; i < e; ++i) {
+    offs[i] = run;
+    cursor[i] = run;
+    run += count[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) offs[n] = run;
+}
+
+// Inverts the probe lists: list[cursor[c]++] = q * probes + r for every
+// probe r of every query q that names cluster c.
+__global__ void cluster_scatter_kernel(const uint32_t *probe, int total, uint32_t *cursor, uint32_t *list) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x)
+    list[atomicAdd(cursor + probe[i], 1u)] = static_cast<uint32_t>(i);
+}
+
+// Two-level choice, second kernel: block c scores cluster c's entries
+// (rows row_offs[c] .. row_offs[c+1] of the cluster-ordered block) against
+// every query that probes it, 32 queries at a time, and writes each
+// (query, probe) pair's NS nearest entries, ascending, to part_*.
+template <int METRIC, int NS>
+__global__ void __launch_bounds__(TB_WARPS * 32) clusters_tiled_kernel(const float *queries, int dim, int dpad,
+                                                                       const float *fine_rows,
+                                                                       const uint32_t *fine_ids,
+                                                                       const uint32_t *row_offs,
+                                                                       const uint32_t *q_offs, const uint32_t *q_list,
+                                                                       int probes, int nbuf, float *part_d,
+                                                                       uint32_t *part_i) {
+  extern __shared__ __align__(16) float smt[];
+  const int c = blockIdx.x;
+  const uint32_t a0 = q_offs[c], a1 = q_offs[c + 1];
+  if (a0 == a1) return;  // no query probes this cluster (uniform over the block)
+  const int r0 = static_cast<int>(row_offs[c]), r1 = static_cast<int>(row_offs[c + 1]);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float *qs = smt;
+  float *xb = smt + static_cast<size_t>(dpad) * TB_QUERIES;
+  const float *qw = qs + static_cast<size_t>(4 * warp) * dpad;
+  for (uint32_t qb = a0; qb < a1; qb += TB_QUERIES) {
+    const int nqb = static_cast<int>(min(static_cast<uint32_t>(TB_QUERIES), a1 - qb));
+    const bool busy = 4 * warp < nqb;  // warp-uniform
+    __syncthreads();  // the previous query tile is no longer read
+    for (int i = threadIdx.x; i < TB_QUERIES * dpad; i += blockDim.x) {
+      const int r = i / dpad, j = i - r * dpad;
+      float v = 0.0f;
+      if (r < nqb && j < dim) v = queries[static_cast<size_t>(q_list[qb + r] / probes) * dim + j];
+      qs[i] = v;
+    }
+    float bd[NS];
+    uint32_t bi[NS];
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      bd[m] = __int_as_float(0x7f800000);
+      bi[m] = 0xffffffffu;
+    }
+    stream_rows(fine_rows, dpad, r0, r1, nbuf, xb, [&](int first, int n, const float *cur) {
+      if (!busy) return;
+      for (int g = 0; g < n; g += 8) {
+        const float d = warp_tile_distance<METRIC>(qw, dpad, cur + static_cast<size_t>(g) * dpad, dpad, dpad, lane);
+        const int r = g + (lane & 7);
+        if (r < n) list_insert<NS>(bd, bi, d, fine_ids[first + r]);
+      }
+    });
+    const int slot = 4 * warp + (lane >> 3);
+    const uint32_t pair = slot < nqb ? q_list[qb + slot] : 0u;
+    int h = 0;
+#pragma unroll
+    for (int r = 0; r < NS; ++r) {
+      float wd;
+      uint32_t wid;
+      group8_take<NS>(bd, bi, h, wd, wid);
+      if ((lane & 7) == 0 && slot < nqb) {
+        part_d[static_cast<size_t>(pair) * NS + r] = wd;
+        part_i[static_cast<size_t>(pair) * NS + r] = wid;
+      }
+    }
   }
 }
 
-// Both kernels on stream s.  `out` holds nq * (ns + probes) words: the
-// starts, then the probed clusters.
-cudaError_t launch_2level(const song_index *ix, const float *queries, int nq, uint32_t *out, cudaStream_t s) {
+// Each query's ns nearest over its probes' lists, ascending by (distance, id).
+template <int NS>
+__global__ void merge_starts_kernel(const float *part_d, const uint32_t *part_i, int nq, int probes, int ns,
+                                    uint32_t *starts) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    float bd[NS];
+    uint32_t bi[NS];
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      bd[m] = __int_as_float(0x7f800000);
+      bi[m] = 0xffffffffu;
+    }
+    const size_t base = static_cast<size_t>(q) * probes * NS;
+    for (int i = 0; i < probes * NS; ++i) list_insert<NS>(bd, bi, part_d[base + i], part_i[base + i]);
+#pragma unroll
+    for (int m = 0; m < NS; ++m)
+      if (m < ns) starts[static_cast<size_t>(q) * ns + m] = bi[m];
+  }
+}
+
+int tiled_nbuf(int dpad) { return tiled_smem(dpad, 2) <= 96u * 1024u ? 2 : 1; }
+
+// Raises a kernel's dynamic shared-memory limit.
+template <class K>
+cudaError_t allow_smem(K kern, size_t bytes) {
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+// The two-level choice on stream s.  `out` holds nq * (ns + probes) words:
+// the starts, then the probed clusters.
+cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t *out, cudaStream_t s) {
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
-  const int tile_bytes = 32 * (dpad / 4 + 1) * 16;
-  const int per_warp = dpad * 4;
-  if (tile_bytes + per_warp > 48 * 1024) return cudaErrorInvalidValue;  // checked at set-up
-  const int nbuf = 2 * tile_bytes + per_warp <= 48 * 1024 ? 2 : 1;
-  const int wpb = std::max(1, std::min(8, (48 * 1024 - nbuf * tile_bytes) / per_warp));
-  const size_t smem_a = static_cast<size_t>(nbuf) * tile_bytes + static_cast<size_t>(per_warp) * wpb;
-  const unsigned grid_a = static_cast<unsigned>((nq + wpb - 1) / wpb);
-  const int ns = ix->n_starts, np = ix->n_probes;
-  uint32_t *probes = out + static_cast<size_t>(nq) * ns;
+  const int ns = ix->n_starts, np = ix->n_probes, coarse = ix->n_coarse;
+  const int nbuf = tiled_nbuf(dpad);
+  const size_t smem = tiled_smem(dpad, nbuf);
   const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
   const int NPsel = np <= 1 ? 1 : (np <= 2 ? 2 : (np <= 4 ? 4 : 8));
-  const unsigned grid_b = static_cast<unsigned>((nq + 1) / 2);
-  const size_t smem_b = static_cast<size_t>(per_warp) * 2;
-#define SONG_HEADS(M, NP)                                                                                   \
-  nearest_head_kernel<M, NP><<<grid_a, 32 * wpb, smem_a, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows, \
-                                                               ix->n_coarse, np, nbuf, probes)
-#define SONG_CLUSTERS(M, NS)                                                                              \
-  nearest_in_clusters_kernel<M, NS><<<grid_b, 64, smem_b, s>>>(queries, nq, dim, dpad, ix->d_entry_rows, \
-                                                                ix->d_entry_ids, ix->d_offsets, probes, np, ns, out)
-#define SONG_2L(M)                          \
-  switch (NPsel) {                          \
-    case 1: SONG_HEADS(M, 1); break;        \
-    case 2: SONG_HEADS(M, 2); break;        \
-    case 4: SONG_HEADS(M, 4); break;        \
-    default: SONG_HEADS(M, 8); break;       \
-  }                                         \
-  switch (NSel) {                           \
-    case 1: SONG_CLUSTERS(M, 1); break;     \
-    case 2: SONG_CLUSTERS(M, 2); break;     \
-    case 4: SONG_CLUSTERS(M, 4); break;     \
-    default: SONG_CLUSTERS(M, 8); break;    \
+  uint32_t *probes = out + static_cast<size_t>(nq) * ns;
+  // work area: cursors, offsets, inverted lists, per-(query, probe) lists
+  const size_t pairs = static_cast<size_t>(nq) * np;
+  const size_t need = static_cast<size_t>(coarse) * 2 + 1 + pairs + 2 * pairs * NSel;
+  if (need > ix->cap_entry_work) {
+    cudaFree(ix->d_entry_work);
+    ix->d_entry_work = nullptr;
+    ix->cap_entry_work = 0;
+    cudaError_t e = cudaMalloc(&ix->d_entry_work, sizeof(uint32_t) * need);
+    if (e != cudaSuccess) return e;
+    ix->cap_entry_work = need;
+  }
+  uint32_t *cursor = ix->d_entry_work;
+  uint32_t *q_offs = cursor + coarse;
+  uint32_t *q_list = q_offs + coarse + 1;
+  float *part_d = reinterpret_cast<float *>(q_list + pairs);
+  uint32_t *part_i = q_list + pairs + pairs * NSel;
+  cudaError_t e = cudaMemsetAsync(ix->d_cl_count, 0, sizeof(uint32_t) * coarse, s);
+  if (e != cudaSuccess) return e;
+  const unsigned grid_q = static_cast<unsigned>((nq + TB_QUERIES - 1) / TB_QUERIES);
+#define SONG_HEADS(M, NP)                                                                                \
+  do {                                                                                                   \
+    auto k_ = heads_tiled_kernel<M, NP>;                                                                 \
+    if ((e = allow_smem(k_, smem)) != cudaSuccess) return e;                                             \
+    k_<<<grid_q, TB_WARPS * 32, smem, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows, coarse, np, nbuf,   \
+                                           probes, ix->d_cl_count);                                      \
+  } while (0)
+#define SONG_CLUSTERS(M, NS)                                                                             \
+  do {                                                                                                   \
+    auto k_ = clusters_tiled_kernel<M, NS>;                                                              \
+    if ((e = allow_smem(k_, smem)) != cudaSuccess) return e;                                             \
+    k_<<<coarse, TB_WARPS * 32, smem, s>>>(queries, dim, dpad, ix->d_entry_rows, ix->d_entry_ids,         \
+                                           ix->d_offsets, q_offs, q_list, np, nbuf, part_d, part_i);     \
+    merge_starts_kernel<NS><<<(nq + 255) / 256, 256, 0, s>>>(part_d, part_i, nq, np, ns, out);           \
+  } while (0)
+#define SONG_HEADS_BY_NP(M)               \
+  switch (NPsel) {                        \
+    case 1: SONG_HEADS(M, 1); break;      \
+    case 2: SONG_HEADS(M, 2); break;      \
+    case 4: SONG_HEADS(M, 4); break;      \
+    default: SONG_HEADS(M, 8); break;     \
+  }
+#define SONG_CLUSTERS_BY_NS(M)            \
+  switch (NSel) {                         \
+    case 1: SONG_CLUSTERS(M, 1); break;   \
+    case 2: SONG_CLUSTERS(M, 2); break;   \
+    case 4: SONG_CLUSTERS(M, 4); break;   \
+    default: SONG_CLUSTERS(M, 8); break;  \
   }
   switch (ix->dx.metric) {
-    case SONG_METRIC_L2: SONG_2L(SONG_METRIC_L2); break;
-    case SONG_METRIC_IP: SONG_2L(SONG_METRIC_IP); break;
-    default: SONG_2L(SONG_METRIC_COS); break;
+    case SONG_METRIC_L2: SONG_HEADS_BY_NP(SONG_METRIC_L2); break;
+    case SONG_METRIC_IP: SONG_HEADS_BY_NP(SONG_METRIC_IP); break;
+    default: SONG_HEADS_BY_NP(SONG_METRIC_COS); break;
   }
-#undef SONG_2L
+  cluster_scan_kernel<<<1, 1024, 0, s>>>(ix->d_cl_count, coarse, q_offs, cursor);
+  cluster_scatter_kernel<<<static_cast<unsigned>(std::min<size_t>((pairs + 255) / 256, 4096)), 256, 0, s>>>(
+      probes, static_cast<int>(pairs), cursor, q_list);
+  switch (ix->dx.metric) {
+    case SONG_METRIC_L2: SONG_CLUSTERS_BY_NS(SONG_METRIC_L2); break;
+    case SONG_METRIC_IP: SONG_CLUSTERS_BY_NS(SONG_METRIC_IP); break;
+    default: SONG_CLUSTERS_BY_NS(SONG_METRIC_COS); break;
+  }
+#undef SONG_CLUSTERS_BY_NS
+#undef SONG_HEADS_BY_NP
 #undef SONG_CLUSTERS
 #undef SONG_HEADS
   return cudaGetLastError();
@@ -609,10 +695,15 @@ void clear_entries(song_index *ix) {
   cudaFree(ix->d_entry_rows);
   cudaFree(ix->d_coarse_rows);
   cudaFree(ix->d_offsets);
+  cudaFree(ix->d_cl_count);
+  cudaFree(ix->d_entry_work);
   ix->d_entry_ids = nullptr;
   ix->d_entry_rows = nullptr;
   ix->d_coarse_rows = nullptr;
   ix->d_offsets = nullptr;
+  ix->d_cl_count = nullptr;
+  ix->d_entry_work = nullptr;
+  ix->cap_entry_work = 0;
   ix->n_entries = 0;
   ix->n_coarse = 0;
   ix->n_probes = 0;
@@ -806,6 +897,8 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
                                                          ix->d_coarse_rows);
     e = cudaGetLastError();
   }
+  // 4. the per-cluster probe counters of the second kernel
+  if (e == cudaSuccess) e = cudaMalloc(&ix->d_cl_count, sizeof(uint32_t) * coarse);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
   cudaFree(d_ids);
   cudaFree(d_rows);

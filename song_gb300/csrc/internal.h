@@ -118,6 +118,9 @@ struct song_index {
   int n_probes = 0;
   float *d_coarse_rows = nullptr;
   uint32_t *d_offsets = nullptr;
+  uint32_t *d_cl_count = nullptr;      // probes per cluster (per call)
+  uint32_t *d_entry_work = nullptr;    // per-call lists of the two-level choice
+  size_t cap_entry_work = 0;
   int servers = 0;  // servers using the entries (song_server_create); they stay fixed meanwhile
   uint32_t *d_starts = nullptr;
   size_t cap_starts = 0;
