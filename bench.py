@@ -5,8 +5,9 @@ One step = one batched search of the workload's query set (10,000 queries)
 over the resident index.  Default workload: 1,000,000 x 128 float32 vectors
 with integer values 0-255 (1,000-centre Gaussian mixture, sigma 20; a
 synthetic stand-in for SIFT1M's shape), L2, degree-32 graph (shift 5,
-FIXED_DEGREE 31, SEARCH_DEGREE 15) built by this project's batch-parallel
-builder, top-10, recall@10 against an FP64 exact kNN (tie-aware).
+FIXED_DEGREE 31, SEARCH_DEGREE 15) built batch-parallel (batch div 64),
+top-10, recall@10 against an FP64 exact kNN (tie-aware, a repeated id counted
+once).
 
 The default mode measures three arms, each at the smallest pq of a sweep
 whose recall@10 reaches the target (0.95), and reports the fastest:
@@ -15,24 +16,33 @@ whose recall@10 reaches the target (0.95), and reports the fastest:
            (two-level choice over sampled entries, song_index_set_entries_2level);
   learned  the learned early exit with BF16 rows and FP32 rerank, from the
            same entries.
+Beside them: the pq sweep 50-400 of the entries arm at top-10 and top-100,
+the top-100 figure, and learned+BF16 against FP32 from the same starts.
 
   value  queries/s of the reported arm's kernels, queries and index resident
          in HBM, CUDA events on the launching stream, L2 flushed between steps.
   e2e    queries/s through song_search (host query buffer in pinned memory,
          host->device copy, search, device->host copy of the ids), host clock.
+  roofline  the search kernel (the step's dominant kernel), timed alone with
+         the library's stage events (song_index_set_timing).
 
-`--impl reference` times the reference's CPU best-first search
-(graph.h:169-216; the oracle's restatement, pinned to the reference's own
-code by tests/golden) on all host cores, at the result size k whose recall@10
-matches the target, on bounded samples of the same workload.  Other modes:
-precision (storage error and recall per row format), serve (Poisson request
-stream against two resident indexes), build (graph construction, GPU vs CPU).
+`--impl reference` runs the reference's own algorithms on the same workload:
+its CPU best-first search (graph.h:169-216, restated in oracle/) on all host
+cores over the same graph (built by the oracle's restatement of the
+reference builder), at the result size k whose recall@10 matches the target;
+and, where the reference's GPU kernel was rebuilt for sm_100 (oracle/_ref),
+that kernel on this GPU at matched recall.  It leaves the latter in the cache
+directory, where the default arm picks it up (same box, run before it).
+Other modes: precision (storage error and recall per row format), serve
+(Poisson request stream against two resident indexes), build (graph
+construction, GPU vs CPU).
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -46,7 +56,9 @@ sys.path.insert(0, ROOT)
 
 PQ_SWEEP = [40, 45, 50, 55, 60, 65, 70, 75, 80, 90, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800,
             1000]
+PQ_TABLE = [50, 75, 100, 150, 200, 250, 300, 400]   # the reported sweep (top-10; top-100 from pq 100)
 CPU_K_SWEEP = [10, 20, 40, 80, 150, 300, 500, 800, 1200, 1600, 2000]
+REF_GPU_PQ = [100, 200, 400, 600, 800, 1000]         # pq values of the rebuilt reference kernel
 
 
 def log(*a):
@@ -68,6 +80,7 @@ def parse_args():
     p.add_argument("--build-div", type=int, default=64)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-table", action="store_true", help="skip the pq 50-400 top-10/top-100 table")
     p.add_argument("--cache", default=os.environ.get("SONG_CACHE", os.path.join(ROOT, "_cache")))
     p.add_argument("--curve", action="store_true", help="time every pq of the sweep (recall/throughput curve)")
     p.add_argument("--mode", choices=["best", "learned", "plain", "entries", "precision", "serve", "build"],
@@ -95,12 +108,37 @@ def parse_args():
     return args
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
+
+
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
 
-def load_workload(args, rank=0, barrier=None, gpu_build=True):
-    import song_gb300 as S
+def graph_path(args, w):
+    return os.path.join(args.cache, "%s.div%d.graph" % (w.name, args.build_div))
+
+
+def load_workload(args, rank=0, barrier=None, builder="gpu"):
+    """Data, queries and the degree-32 graph (cached).  builder: "gpu" (the
+    product's GPU builder), "cpu" (its CPU builder) or "oracle" (the oracle's
+    restatement of the reference builder); all three write the same graph
+    bit for bit (tests/test_graph_build_gpu.py, tests/test_oracle_golden.py)."""
     from song_gb300 import datasets as D
     w = D.WORKLOADS[args.workload]
     nq = args.nq or w.n_queries
@@ -109,41 +147,47 @@ def load_workload(args, rank=0, barrier=None, gpu_build=True):
     queries = D.query_vectors(w, nq=nq)
     log("[bench] %s: data %s queries %s in %.1fs" % (w.name, data.shape, queries.shape, time.time() - t))
     os.makedirs(args.cache, exist_ok=True)
-    gpath = os.path.join(args.cache, "%s.div%d.graph" % (w.name, args.build_div))
+    gpath = graph_path(args, w)
     if rank == 0 and not os.path.exists(gpath):
-        # The GPU builder writes the CPU builder's graph bit for bit
-        # (tests/test_graph_build_gpu.py), in a third of the time.
         t = time.time()
-        if gpu_build:
-            g = S.graph_build_gpu(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
-                                  batch_div=args.build_div, device=int(os.environ.get("LOCAL_RANK", "0")),
-                                  nthreads=os.cpu_count())
+        bargs = (data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150)
+        if builder == "oracle":
+            from oracle import oracle as O
+            g = O.graph_build(*bargs, batch_div=args.build_div, nthreads=os.cpu_count())
         else:
-            g = S.graph_build(data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150,
-                              batch_div=args.build_div, nthreads=os.cpu_count())
+            import song_gb300 as S
+            fn = S.graph_build_gpu if builder == "gpu" else S.graph_build
+            kw = {"device": int(os.environ.get("LOCAL_RANK", "0"))} if builder == "gpu" else {}
+            g = fn(*bargs, batch_div=args.build_div, nthreads=os.cpu_count(), **kw)
         tmp = gpath + ".tmp%d" % os.getpid()
         g.tofile(tmp)
         os.replace(tmp, gpath)
         log("[bench] graph built in %.1fs (%s builder, batch_div %d, %d threads)"
-            % (time.time() - t, "GPU" if gpu_build else "CPU", args.build_div, os.cpu_count()))
+            % (time.time() - t, builder, args.build_div, os.cpu_count()))
     if barrier:
         barrier()
     graph = np.fromfile(gpath, dtype=np.uint64)
     return w, data, queries, graph
 
 
-def ground_truth(args, w, data, queries, k):
+def ground_truth(args, w, data, queries, k, device=None):
+    """Exact k nearest ids and the exact 10th and k-th distances (FP64)."""
     from song_gb300 import groundtruth as GT
     path = os.path.join(args.cache, "%s.nq%d.k%d.gt.npz" % (w.name, queries.shape[0], k))
     if os.path.exists(path):
         z = np.load(path)
-        return z["ids"], z["kth"]
+        return z["ids"], z["kth"], z["kth10"]
     t = time.time()
-    ids, kth = GT.exact_knn_fp64(data, queries, k, w.metric)
-    np.savez(path, ids=ids, kth=kth)
-    log("[bench] fp64 exact kNN in %.1fs" % (time.time() - t))
-    return ids, kth
+    ids, kth = GT.exact_knn_fp64(data, queries, k, w.metric, device=device)
+    kth10 = GT.distances_fp64(data, queries, ids[:, min(k, 10) - 1:min(k, 10)], w.metric)[:, 0]
+    np.savez(path, ids=ids, kth=kth, kth10=kth10)
+    log("[bench] fp64 exact kNN (k=%d) in %.1fs" % (k, time.time() - t))
+    return ids, kth, kth10
 
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
 
 # ---------------------------------------------------------------------------
 # clocks
@@ -211,11 +255,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows), "samples_under_load": len(loaded)}
 
 
+
 # ---------------------------------------------------------------------------
-# CPU reference search (oracle restatement of graph.h:169-216)
+# the reference's algorithms (oracle/): CPU search, and its GPU kernel rebuilt
+# for sm_100
 # ---------------------------------------------------------------------------
 
-def cpu_calibrate_k(w, data, graph, queries, target, gt_ids, gt_kth, sample=400):
+def cpu_calibrate_k(w, data, graph, queries, target, gt_kth10, sample=400):
     from oracle import oracle as O
     from song_gb300 import groundtruth as GT
     ox = O.OracleIndex(data, graph, w.shift, O.METRICS[w.metric])
@@ -225,7 +271,7 @@ def cpu_calibrate_k(w, data, graph, queries, target, gt_ids, gt_kth, sample=400)
         if k < 10:
             continue
         ids, _ = ox.cpu_search(qs, k)
-        r = GT.recall_tie_aware(ids, data, qs, gt_kth[:sample], w.metric, 10)
+        r = GT.recall_tie_aware(ids, data, qs, gt_kth10[:sample], w.metric, 10)
         sweep.append((k, round(r, 4)))
         if r >= target:
             return k, sweep
@@ -249,40 +295,102 @@ def cpu_time(w, data, graph, queries, k, seconds, nthreads):
     return n / dt, n, dt
 
 
+def reference_kernel_sm100(w, data, graph, queries, gt_kth10, target):
+    """The reference's own GPU kernel (warp_astar_accelerator.h:41-341)
+    rebuilt for sm_100 (oracle/_ref cubins), on this GPU: queries/s of each
+    available pq_size (the faster of __ENABLE_MEASURE as shipped and
+    removed) and the smallest pq whose recall@10 reaches the target."""
+    from oracle import ref_gpu
+    from song_gb300 import groundtruth as GT
+    metric = w.metric
+    pqs = [pq for pq in REF_GPU_PQ if ref_gpu.available(metric, w.dim, pq)]
+    if not pqs:
+        return {"unavailable": "reference cubins not built on this host (oracle/build_ref_gpu.sh)"}
+    nq = queries.shape[0]
+    rows = []
+    chosen = None
+    for pq in pqs:
+        best = None
+        for measure in (True, False):
+            ids, ms = ref_gpu.run(ref_gpu.cubin_path(metric, w.dim, pq, measure), data, graph, w.shift, queries, pq,
+                                  measure, repeats=3, heap_pq=max(pqs))
+            qps = nq / (float(np.median(ms)) / 1000.0)
+            if best is None or qps > best["qps"]:
+                rec = GT.recall_tie_aware(ids[:, :10], data, queries, gt_kth10, metric, 10)
+                best = {"pq": pq, "qps": round(qps, 1), "recall_at_10": round(rec, 4),
+                        "measure_build": measure, "kernel_ms_median": round(float(np.median(ms)), 3)}
+        rows.append(best)
+        log("[reference sm_100] %s" % best)
+        if chosen is None and best["recall_at_10"] >= target:
+            chosen = best
+    return {"at_target": chosen, "sweep": rows, "queries": nq,
+            "kernel": "warp_astar_accelerator.h:41-341 rebuilt for sm_100 (compute_100), one launch per batch"}
+
+
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU search on all host cores."""
+    """--impl reference: the reference's CPU search on all host cores, over the
+    same graph (the oracle's builder), and its GPU kernel rebuilt for sm_100."""
     if rank != 0:
         return
     from oracle import oracle as O
     O.build()
-    w, data, queries, graph = load_workload(args, gpu_build=False)
+    w, data, queries, graph = load_workload(args, builder="oracle")
     from song_gb300 import groundtruth as GT
     sample = min(400, queries.shape[0])
-    gt_ids, gt_kth = GT.exact_knn_fp64(data, queries[:sample], args.topk, w.metric, device="cpu")
-    k, sweep = cpu_calibrate_k(w, data, graph, queries, args.recall, gt_ids, gt_kth, sample)
+    _, _, kth10 = ground_truth(args, w, data, queries[:sample], args.topk, device="cpu")
+    k, sweep = cpu_calibrate_k(w, data, graph, queries, args.recall, kth10, sample)
     nthreads = os.cpu_count() or 1
-    per_step = max(1.0, 150.0 / max(1, args.steps + args.warmup))
-    for _ in range(args.warmup):
-        cpu_time(w, data, graph, queries, k, per_step / 4, nthreads)
-    total_q, total_t = 0, 0.0
-    for _ in range(args.steps):
-        rate, n, dt = cpu_time(w, data, graph, queries, k, per_step, nthreads)
-        total_q += n
-        total_t += dt
-    value = total_q / total_t
+    nq = queries.shape[0]
+    ox = O.OracleIndex(data, graph, w.shift, O.METRICS[w.metric])
+    # a step searches a bounded slice of the workload's queries, sized so the
+    # whole run takes about a minute and a half of CPU time
+    rate, _, _ = cpu_time(w, data, graph, queries, k, 2.0, nthreads)
+    per_step = int(max(64, min(nq, rate * 90.0 / max(1, args.steps + args.warmup))))
+    for i in range(args.warmup):
+        ox.cpu_search(queries[:per_step], k, nthreads=nthreads)
+    times = []
+    for i in range(args.steps):
+        a = (i * per_step) % nq
+        qs = queries[np.arange(a, a + per_step) % nq]
+        t = time.perf_counter()
+        ox.cpu_search(qs, k, nthreads=nthreads)
+        times.append(time.perf_counter() - t)
+    value = per_step * args.steps / sum(times)
+    ref_gpu = None
+    try:
+        import torch
+        if torch.cuda.is_available():
+            _, _, kth10_all = ground_truth(args, w, data, queries, 100)
+            ref_gpu = reference_kernel_sm100(w, data, graph, queries, kth10_all, args.recall)
+            with open(os.path.join(args.cache, "%s.reference_sm100.json" % w.name), "w") as f:
+                json.dump(ref_gpu, f)
+    except Exception as e:  # the CPU baseline is this arm's value; the GPU kernel is context
+        ref_gpu = {"error": repr(e)}
     line = {
-        "impl": "reference", "metric": "queries/s at recall@10>=%.2f, %s" % (args.recall, w.name), "value": round(value, 1),
-        "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * total_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64-accumulated f32", "data": "synthetic",
-        "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric, "graph_shift": w.shift,
-                   "search": "CPU best-first search graph.h:169-216 (oracle restatement)",
-                   "k": k, "recall_sweep_k": sweep, "queries_per_step": total_q // args.steps},
+        "impl": "reference", "metric": "queries/s at recall@10>=%.2f, %s" % (args.recall, w.name),
+        "value": round(value, 1), "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 data, f64-accumulated distances", "data": "synthetic",
+        "config": common_config(args, w, nq),
+        "arm": {"name": "reference CPU best-first search (graph.h:169-216, oracle restatement), vertex-0 start",
+                "k": k, "recall_sweep_k": sweep, "queries_per_step": per_step,
+                "graph": "oracle/song_oracle.c orc_graph_build (the reference builder, batch div %d), equal to the "
+                         "product builder's graph" % args.build_div},
         "cpu_baseline": {"value": round(value, 1), "unit": "queries/s", "cores": nthreads, "kind": "port",
-                         "sample": "%d queries per step (workload query set repeated), k=%d" % (total_q // args.steps, k)},
+                         "cpu_model": cpu_model(),
+                         "sample": "%d queries per step (slices of the workload's query set), k=%d" % (per_step, k)},
+        "reference_kernel_sm100": ref_gpu,
         "e2e": {"value": round(value, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def common_config(args, w, nq):
+    """The workload description, the same in both arms' lines."""
+    return {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric, "top_k": args.topk,
+            "recall_target": args.recall, "queries": nq,
+            "graph": "shift %d (FIXED_DEGREE %d, SEARCH_DEGREE %d), budget 150, batch div %d"
+                     % (w.shift, w.fixed_degree, w.search_degree, args.build_div)}
 
 
 # ---------------------------------------------------------------------------
@@ -311,23 +419,31 @@ class Runner:
         return self.out.cpu().numpy().view(np.uint64)
 
 
-def timed_steps(torch, run, pq, steps, flush, stream):
+def timed_steps(torch, run, pq, steps, flush, stream, stage=None):
+    """Per-step ms of `steps` searches (CUDA events on the launching stream,
+    L2 flushed before each); with stage (the index, timing enabled) also the
+    entry-choice and search-kernel ms of each step."""
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    st = []
     for i in range(steps):
         flush.zero_()
         ev[i][0].record(stream)
         run(pq)
         ev[i][1].record(stream)
+        if stage is not None:
+            st.append(stage.timing())
     torch.cuda.synchronize()
-    return [a.elapsed_time(b) for a, b in ev]
+    return [a.elapsed_time(b) for a, b in ev], st
 
 
-def sweep_pq(torch, run, w, data, queries, gt_kth, k, target, curve, log_prefix):
-    """Smallest pq of PQ_SWEEP whose tie-aware recall@k reaches target."""
+def sweep_pq(torch, run, w, data, queries, gt_kth, k, target, curve, log_prefix, sweep=PQ_SWEEP):
+    """Smallest pq of the sweep whose tie-aware recall@k reaches target."""
     from song_gb300 import groundtruth as GT
     nq = queries.shape[0]
     out, chosen = [], 0
-    for cand in PQ_SWEEP:
+    for cand in sweep:
+        if cand < k:
+            continue
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         run(cand)
         t0.record(run.stream)
@@ -339,12 +455,12 @@ def sweep_pq(torch, run, w, data, queries, gt_kth, k, target, curve, log_prefix)
         qps = reps * nq / (t0.elapsed_time(t1) / 1000.0)
         r = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
         out.append([cand, round(r, 4), round(qps, 1)])
-        log("[bench] %s pq %d recall@10 %.4f  %.0f q/s" % (log_prefix, cand, r, qps))
+        log("[bench] %s pq %d recall@%d %.4f  %.0f q/s" % (log_prefix, cand, k, r, qps))
         if not chosen and r >= target:
             chosen = cand
             if not curve:
                 break
-    return (chosen or PQ_SWEEP[-1]), out
+    return (chosen or sweep[-1]), out
 
 
 # ---------------------------------------------------------------------------
@@ -374,7 +490,7 @@ def run_precision(args, torch, local):
     from song_gb300 import groundtruth as GT
     w, data, queries, graph = load_workload(args)
     nq, k = queries.shape[0], args.topk
-    gt_ids, gt_kth = ground_truth(args, w, data, queries, k)
+    gt_ids, gt_kth, _ = ground_truth(args, w, data, queries, k)
     stream = torch.cuda.current_stream()
     dq = torch.from_numpy(queries).cuda()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -567,36 +683,63 @@ def run_build(args, torch, local):
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse_args()
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        run_reference(args, rank, world)
-        return
+# ---------------------------------------------------------------------------
+# the default mode: plain / entries / learned arms
+# ---------------------------------------------------------------------------
 
-    import torch
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    if args.mode == "precision":
-        run_precision(args, torch, local)
-        return
-    if args.mode == "serve":
-        run_serve(args, torch, local)
-        return
-    if args.mode == "build":
-        run_build(args, torch, local)
-        return
+def measure_arm(torch, run, pq, steps, flush, stream, data, queries, kth10, w):
+    """recall@10, hops, evaluations and kernel queries/s of one arm at pq."""
+    from song_gb300 import groundtruth as GT
+    run(pq, stats=True)
+    rec = GT.recall_tie_aware(run.ids(), data, queries, kth10, w.metric, 10)
+    hops = float(run.hops.float().mean().item())
+    evals = float(run.evals.float().mean().item())
+    for _ in range(2):
+        run(pq)
+    ms, _ = timed_steps(torch, run, pq, steps, flush, stream)
+    med = statistics.median(ms)
+    return {"qps": round(queries.shape[0] / (med / 1000.0), 1), "pq": pq, "recall_at_10": round(rec, 4),
+            "kernel_ms_median": round(med, 4), "mean_hops": round(hops, 2), "mean_evals": round(evals, 2)}
 
-    def barrier():
-        if dist:
-            dist.barrier()
 
+def pq_table(torch, ix, dq, stream, flush, data, queries, kth10, kth100, w, target):
+    """The pq sweep 50-400 at top-10 and (pq >= 100) top-100: recall and
+    kernel queries/s; and the smallest pq whose recall@100 reaches target."""
+    from song_gb300 import groundtruth as GT
+    nq = queries.shape[0]
+    r10, r100 = Runner(ix, dq, 10, stream), Runner(ix, dq, 100, stream)
+    rows, top100 = [], None
+    for pq in PQ_TABLE:
+        row = {"pq": pq}
+        for k, run, kth in ((10, r10, kth10), (100, r100, kth100)):
+            if pq < k:
+                continue
+            run(pq)
+            rec = GT.recall_tie_aware(run.ids(), data, queries, kth, w.metric, k)
+            ms, _ = timed_steps(torch, run, pq, 3, flush, stream)
+            row["recall_at_%d" % k] = round(rec, 4)
+            row["qps_top%d" % k] = round(nq / (statistics.median(ms) / 1000.0), 1)
+        rows.append(row)
+        log("[bench] table %s" % row)
+        if top100 is None and row.get("recall_at_100", 0.0) >= target:
+            top100 = {"pq": pq, "recall_at_100": row["recall_at_100"], "qps": row["qps_top100"]}
+    return rows, top100
+
+
+def plain_arm(torch, S, args, w, graph, data, queries, kth10, dq, k, stream, flush, local, msteps):
+    t = time.time()
+    ix32 = S.Index(graph, data, w.shift, w.metric, device=local)
+    log("[bench] FP32 index resident (%.2f GB) in %.1fs" % (ix32.device_bytes() / 1e9, time.time() - t))
+    run32 = Runner(ix32, dq, k, stream)
+    pq32, sweep32 = (args.pq, []) if args.pq else sweep_pq(torch, run32, w, data, queries, kth10, k, args.recall,
+                                                            args.curve, "fp32")
+    plain = measure_arm(torch, run32, pq32, msteps, flush, stream, data, queries, kth10, w)
+    plain["pq_sweep_recall_qps"] = sweep32
+    log("[bench] plain FP32: %s" % plain)
+    return plain, ix32, run32
+
+
+def run_search(args, torch, rank, world, local, dist):
     import ctypes
 
     import song_gb300 as S
@@ -604,124 +747,117 @@ def main():
     from song_gb300 import groundtruth as GT
     from song_gb300 import learned as LE
     from song_gb300 import replicas as R
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
     S.load_library()
     w, data, queries, graph = load_workload(args, rank, barrier)
     nq, k = queries.shape[0], args.topk
-    gt_ids, gt_kth = ground_truth(args, w, data, queries, k)
+    gt_ids, kth100, kth10 = ground_truth(args, w, data, queries, 100)
     stream = torch.cuda.current_stream()
     dq = torch.from_numpy(queries).cuda()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    msteps = max(3, args.steps // 2)
+    entries = S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True) if args.entries > 0 else None
 
-    # ---- plain FP32 search (the reference's semantics) ----------------------
-    t = time.time()
-    ix32 = S.Index(graph, data, w.shift, w.metric, device=local)
-    log("[bench] FP32 index resident (%.2f GB) in %.1fs" % (ix32.device_bytes() / 1e9, time.time() - t))
-    run32 = Runner(ix32, dq, k, stream)
-    pq32, sweep32 = (args.pq, []) if args.pq else sweep_pq(torch, run32, w, data, queries, gt_kth, k, args.recall,
-                                                            args.curve, "fp32")
-    run32(pq32, stats=True)
-    rec32 = GT.recall_tie_aware(run32.ids(), data, queries, gt_kth, w.metric, k)
-    ms32 = timed_steps(torch, run32, pq32, max(3, args.steps // 2), flush, stream)
-    plain = {"qps": round(nq / (statistics.median(ms32) / 1000.0), 1), "pq": pq32, "recall_at_10": round(rec32, 4),
-             "kernel_ms_median": round(statistics.median(ms32), 4),
-             "mean_hops": round(float(run32.hops.float().mean().item()), 2),
-             "mean_evals": round(float(run32.evals.float().mean().item()), 2), "pq_sweep_recall_qps": sweep32}
-    log("[bench] plain FP32: %s" % plain)
+    def with_entries(ix):
+        if entries is not None:
+            ix.set_entries(entries, starts=args.starts, coarse=args.coarse, probes=args.probes)
 
-    # ---- the same search from the nearest entry point (option) ---------------
-    ent = None
-    if args.mode in ("best", "entries") and args.entries > 0:
+    # ---- plain FP32 search from vertex 0 (the reference's semantics) --------
+    plain, ix32, run32 = None, None, None
+    if args.mode in ("best", "plain") or entries is None:
+        plain, ix32, run32 = plain_arm(torch, S, args, w, graph, data, queries, kth10, dq, k, stream, flush, local,
+                                       msteps)
+
+    # ---- the same search from each query's nearest entry vertices ----------
+    ent, ixe, rune, table, top100 = None, None, None, [], None
+    if args.mode in ("best", "entries", "learned") and entries is not None:
         ixe = S.Index(graph, data, w.shift, w.metric, device=local)
-        ixe.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True), starts=args.starts,
-                        coarse=args.coarse, probes=args.probes)
+        with_entries(ixe)
         rune = Runner(ixe, dq, k, stream)
-        pqe, sweepe = (args.pq, []) if args.pq else sweep_pq(torch, rune, w, data, queries, gt_kth, k, args.recall,
+        pqe, sweepe = (args.pq, []) if args.pq else sweep_pq(torch, rune, w, data, queries, kth10, k, args.recall,
                                                               args.curve, "fp32+entries")
-        rune(pqe, stats=True)
-        rece = GT.recall_tie_aware(rune.ids(), data, queries, gt_kth, w.metric, k)
-        mse = timed_steps(torch, rune, pqe, max(3, args.steps // 2), flush, stream)
-        ent = {"qps": round(nq / (statistics.median(mse) / 1000.0), 1), "pq": pqe, "recall_at_10": round(rece, 4),
-               "entries": args.entries, "starts_per_query": args.starts, "coarse": args.coarse,
-               "probes": args.probes, "kernel_ms_median": round(statistics.median(mse), 4),
-               "mean_hops": round(float(rune.hops.float().mean().item()), 2),
-               "mean_evals": round(float(rune.evals.float().mean().item()), 2), "pq_sweep_recall_qps": sweepe}
+        ent = measure_arm(torch, rune, pqe, msteps, flush, stream, data, queries, kth10, w)
+        ent.update({"entries": args.entries, "starts_per_query": args.starts, "coarse": args.coarse,
+                    "probes": args.probes, "pq_sweep_recall_qps": sweepe})
         log("[bench] FP32 from entries: %s" % ent)
+    if not args.no_table:
+        table, top100 = pq_table(torch, ixe or ix32, dq, stream, flush, data, queries, kth10, kth100, w, args.recall)
 
-    # ---- learned early exit + BF16 storage + FP32 rerank ----------------------
-    mode = "learned" if args.mode in ("best", "learned") else "plain"
-    if mode == "learned":
-        ix = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
-        ix.set_rerank(args.rerank)
-        if args.entries > 0:  # the same entry points as the entries arm (traces start there too)
-            ix.set_entries(S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True),
-                           starts=args.starts, coarse=args.coarse, probes=args.probes)
-        run = Runner(ix, dq, k, stream)
+    # ---- learned early exit + BF16 storage + FP32 rerank, same starts --------
+    lrn, ixl, runl, model = None, None, None, None
+    if args.mode in ("best", "learned"):
+        ixl = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
+        ixl.set_rerank(args.rerank)
+        with_entries(ixl)
+        runl = Runner(ixl, dq, k, stream)
         train_q = D.query_vectors(w, nq=args.train_queries, seed=D.SEED_TRAIN)
-        pq0 = min(pq32, ent["pq"]) if ent else pq32
-        pq, model, lrec = pq0, None, 0.0
+        pq0 = ent["pq"] if ent else plain["pq"]
         tried = []
-        for cand in [c for c in PQ_SWEEP + [1023] if c >= pq0][:3]:
-            model = LE.fit(ix, train_q, cand, k, epochs=6, data=data, metric=w.metric,
+        for cand in [c for c in PQ_SWEEP + [1023] if c >= pq0][:4]:
+            model = LE.fit(ixl, train_q, cand, k, epochs=6, data=data, metric=w.metric,
                            recall_slack=args.recall_slack, log=log)
-            ix.set_early_exit(model.params, model.threshold, model.min_hops, model.every)
-            run(cand, stats=True)
-            lrec = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
+            ixl.set_early_exit(model.params, model.threshold, model.min_hops, model.every)
+            runl(cand, stats=True)
+            lrec = GT.recall_tie_aware(runl.ids(), data, queries, kth10, w.metric, k)
             tried.append([cand, round(model.threshold, 2), round(lrec, 4)])
             log("[bench] learned+bf16 pq %d threshold %.2f recall@10 %.4f" % (cand, model.threshold, lrec))
-            pq = cand
             if lrec >= args.recall:
                 break
-        rec = lrec
-        for _ in range(2):
-            run(pq)
-        lms = timed_steps(torch, run, pq, 3, flush, stream)
-        learned_qps = nq / (statistics.median(lms) / 1000.0)
-        log("[bench] learned+bf16: %.1f q/s at recall@10 %.4f (plain FP32 %.1f q/s)" % (learned_qps, rec, plain["qps"]))
-        ixl, learned_pq, learned_rec = ix, pq, rec
-    else:
-        ix, run, pq, rec, model, tried = ix32, run32, pq32, rec32, None, []
-        ixl, learned_qps, learned_pq, learned_rec = None, None, None, None
-    # the arm reported: the one asked for, or the fastest that reaches the target
-    arms = {"plain": (plain["qps"], plain["recall_at_10"])}
+        lrn = measure_arm(torch, runl, cand, msteps, flush, stream, data, queries, kth10, w)
+        lrn.update({"threshold": model.threshold, "min_hops": model.min_hops, "rerank": args.rerank,
+                    "train_queries": args.train_queries, "recall_slack": args.recall_slack,
+                    "tried_pq_threshold_recall": tried,
+                    "train": {kk: model.info[kk] for kk in ("samples", "positive", "trace_s", "train_s", "losses",
+                                                            "chosen")}})
+        log("[bench] learned+bf16: %s" % lrn)
+
+    # ---- the arm reported: the one asked for, or the fastest at the target ---
+    arms = {}
+    if plain:
+        arms["plain"] = (plain, ix32, run32)
     if ent:
-        arms["entries"] = (ent["qps"], ent["recall_at_10"])
-    if learned_qps is not None:
-        arms["learned"] = (learned_qps, learned_rec)
-    if args.mode == "best":
-        ok = [a for a in arms if arms[a][1] >= args.recall] or ["plain"]
-        mode = max(ok, key=lambda a: arms[a][0])
-    elif args.mode in arms:
+        arms["entries"] = (ent, ixe, rune)
+    if lrn:
+        arms["learned"] = (lrn, ixl, runl)
+    if args.mode in arms:
         mode = args.mode
-    if mode == "plain":
-        ix, run, pq, rec = ix32, run32, pq32, rec32
-    elif mode == "entries":
-        ix, run, pq, rec = ixe, rune, ent["pq"], rece
-    log("[bench] arms (q/s, recall@10): %s -> %s" % (arms, mode))
+    else:
+        ok = [a for a in arms if arms[a][0]["recall_at_10"] >= args.recall] or list(arms)
+        mode = max(ok, key=lambda a: arms[a][0]["qps"])
+    rep, ix, run = arms[mode]
+    pq = rep["pq"]
+    log("[bench] arms (q/s, recall@10): %s -> %s"
+        % ({a: (v[0]["qps"], v[0]["recall_at_10"]) for a, v in arms.items()}, mode))
     run(pq, stats=True)
     hops = run.hops.cpu().numpy().astype(np.int64)
     evals = run.evals.cpu().numpy().astype(np.int64)
     ids = run.ids()
+    rec = GT.recall_tie_aware(ids, data, queries, kth10, w.metric, k)
     rec_ids = GT.recall(ids, gt_ids, k)
 
+    # ---- timed region ---------------------------------------------------------
+    ix.set_timing(True)
     sampler = ClockSampler(local)
     sampler.start()
-    t0 = time.time()
-    wsteps = 0
-    while wsteps < args.warmup or time.time() - t0 < 1.5:
+    for _ in range(args.warmup):
         flush.zero_()
         run(pq)
-        wsteps += 1
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    kernel_ms = timed_steps(torch, run, pq, args.steps, flush, stream)
+    kernel_ms, stages = timed_steps(torch, run, pq, args.steps, flush, stream, stage=ix)
     wall = time.perf_counter() - wall0
     barrier()
+    ix.set_timing(False)
     total_s = R.max_over_ranks(sum(kernel_ms) / 1000.0, dist, "cuda")
     value = R.whole_job_rate(nq, args.steps, world, total_s)
 
-    # e2e: host buffers through song_search (pinned query buffer)
+    # e2e: host buffers through song_search (pinned query and id buffers)
     pinned = torch.empty((nq, w.dim), dtype=torch.float32, pin_memory=True)
     pinned.numpy()[:] = queries
     hq = pinned.numpy()
@@ -743,10 +879,7 @@ def main():
     e2e_s = R.max_over_ranks(sum(e2e_times), dist, "cuda")
     e2e = R.whole_job_rate(nq, args.steps, world, e2e_s)
 
-    # roofline: algorithmic bytes per launch / mean kernel time
-    entry_bytes = 0
-    if mode == "entries":  # the entry rows, read once per launch (they stay in L2)
-        entry_bytes = args.entries * 4 * (((w.dim + 3) // 4) * 4)
+    # ---- roofline of the search kernel (the step's dominant kernel) ----------
     if mode == "learned":
         row_bytes = 2 * (((w.dim + 7) // 8) * 8)
         rerank_rows = min(args.rerank if args.rerank > 0 else pq, pq)
@@ -754,22 +887,25 @@ def main():
         row_bytes = 4 * (((w.dim + 3) // 4) * 4)
         rerank_rows = 0
     alg_bytes = int((4 * w.dim * nq) + hops.sum() * (1 << w.shift) * 4 + evals.sum() * row_bytes
-                    + nq * rerank_rows * 4 * w.dim + nq * k * 8 + entry_bytes)
-    mean_s = (sum(kernel_ms) / len(kernel_ms)) / 1000.0
-    achieved = alg_bytes / mean_s / 1e9
+                    + nq * rerank_rows * 4 * w.dim + nq * k * 8)
+    entry_ms = [a for a, _ in stages]
+    search_ms = [b for _, b in stages]
+    mean_search_s = statistics.fmean(search_ms) / 1000.0
+    achieved = alg_bytes / mean_search_s / 1e9
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
+    traffic, traffic_src = None, None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         try:
-            tj = json.load(open(tp)).get("%s/%s/pq%d" % (w.name, mode, pq))
+            tj = json.load(open(tp)).get("%s/%s/pq%d" % (w.name, mode, pq), {}).get("search_kernel")
             if tj:
-                traffic = int(tj["dram_bytes_per_query"] * nq)
+                traffic = int(round(tj["dram_bytes"] * nq / tj["queries"]))
+                traffic_src = tj.get("source")
         except Exception:
             traffic = None
 
@@ -779,68 +915,111 @@ def main():
             from oracle import oracle as O
             O.build()
             sample = min(400, nq)
-            ck, csweep = cpu_calibrate_k(w, data, graph, queries, args.recall, gt_ids, gt_kth, sample)
+            ck, csweep = cpu_calibrate_k(w, data, graph, queries, args.recall, kth10, sample)
             nthreads = os.cpu_count() or 1
-            rate, n, dt = cpu_time(w, data, graph, queries, ck, args.cpu_seconds, nthreads)
-            cpu = {"value": round(rate, 1), "unit": "queries/s", "cores": nthreads, "kind": "port",
-                   "sample": "%d queries (workload set repeated), k=%d for recall@10>=%.2f, %.1fs" % (n, ck, args.recall, dt),
+            crate, n, dt = cpu_time(w, data, graph, queries, ck, args.cpu_seconds, nthreads)
+            cpu = {"value": round(crate, 1), "unit": "queries/s", "cores": nthreads, "kind": "port",
+                   "cpu_model": cpu_model(),
+                   "sample": "%d queries (workload set repeated), k=%d for recall@10>=%.2f, %.1fs"
+                             % (n, ck, args.recall, dt),
                    "recall_sweep_k": csweep}
         except Exception as e:  # the baseline must not hide the GPU number
             cpu = {"value": None, "error": repr(e)}
 
+    ref_sm100 = None
+    rp = os.path.join(args.cache, "%s.reference_sm100.json" % w.name)
+    if os.path.exists(rp):
+        try:
+            r = json.load(open(rp))
+            if r.get("at_target"):
+                ref_sm100 = dict(r["at_target"], source="bench.py --impl reference on this machine")
+        except Exception:
+            ref_sm100 = None
+
     if rank == 0:
-        desc = {"learned": "learned early exit + BF16 storage + FP32 rerank"
-                           + (", from the nearest %d of %d entry vertices" % (args.starts, args.entries)
-                              if args.entries > 0 else ""),
-                "entries": "FP32 search from the nearest %d of %d entry vertices%s" % (
-                    args.starts, args.entries,
-                    " (%d clusters, %d probed)" % (args.coarse, args.probes) if args.coarse else ""),
-                "plain": "plain FP32 search"}[mode]
+        desc = {"learned": "learned early exit + BF16 storage + FP32 rerank, from the nearest %d of %d entry "
+                           "vertices" % (args.starts, args.entries),
+                "entries": "FP32 search from the nearest %d of %d entry vertices (%d clusters, %d probed)"
+                           % (args.starts, args.entries, args.coarse, args.probes),
+                "plain": "plain FP32 search from vertex 0"}[mode]
+        same = None
+        if lrn and ent:
+            same = {"learned_bf16": {kk: lrn[kk] for kk in ("qps", "pq", "recall_at_10", "mean_hops")},
+                    "fp32": {kk: ent[kk] for kk in ("qps", "pq", "recall_at_10", "mean_hops")},
+                    "ratio": round(lrn["qps"] / ent["qps"], 3),
+                    "both_at_target": lrn["recall_at_10"] >= args.recall and ent["recall_at_10"] >= args.recall}
+        config = common_config(args, w, nq)
+        config.update({
+            "learned_vs_fp32_same_starts": same,
+            "reference_sm100_qps": ref_sm100["qps"] if ref_sm100 else None,
+            "reference_sm100": ref_sm100,
+            "plain_fp32_vs_reference_sm100": round(plain["qps"] / ref_sm100["qps"], 3) if ref_sm100 and plain
+            else None,
+            "top100": top100,
+            "pq_table": table,
+            "l2": "flushed between steps (256 MB write); index > L2",
+            "parallelism": "replicas" if world > 1 else "single GPU"})
         line = {
             "metric": "queries/s at recall@10>=%.2f, %s" % (args.recall, w.name),
             "value": round(value, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-            "warmup": wsteps, "ms_per_step": round(1000 * total_s / args.steps, 4),
+            "warmup": args.warmup, "ms_per_step": round(1000 * total_s / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16 storage, f32 accumulate, f32 rerank" if mode == "learned" else "f32",
             "data": "synthetic (seeded Gaussian mixture, SIFT1M shape)",
-            "config": {"workload": w.name, "arm": desc, "n": w.n, "dim": w.dim, "metric": w.metric,
-                       "graph": "shift %d (FIXED_DEGREE %d, SEARCH_DEGREE %d), batch-parallel build div %d"
-                                % (w.shift, w.fixed_degree, w.search_degree, args.build_div),
-                       "mode": mode, "pq": pq, "top_k": k, "queries_per_step": nq,
-                       "recall_at_10": round(rec, 4), "recall_at_10_ids": round(rec_ids, 4),
-                       "mean_hops": round(float(hops.mean()), 2), "mean_evals": round(float(evals.mean()), 2),
-                       "plain_fp32": plain,
-                       "fp32_from_entries": ent,
-                       "speedup_vs_plain_fp32": round(value / plain["qps"], 3),
-                       "learned": None if model is None else {
-                           "qps": round(learned_qps, 1), "pq": learned_pq, "recall_at_10": round(learned_rec, 4),
-                           "speedup_vs_plain_fp32": round(learned_qps / plain["qps"], 3),
-                           "threshold": model.threshold, "min_hops": model.min_hops, "rerank": args.rerank,
-                           "train_queries": args.train_queries, "recall_slack": args.recall_slack,
-                           "tried_pq_threshold_recall": tried,
-                           "train": {kk: model.info[kk] for kk in ("samples", "positive", "trace_s", "train_s", "losses", "chosen")}},
-                       "l2": "flushed between steps (256 MB write); index > L2",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": config,
+            "arm": {"name": desc, "mode": mode, "pq": pq, "recall_at_10": round(rec, 4),
+                    "recall_at_10_ids": round(rec_ids, 4), "mean_hops": round(float(hops.mean()), 2),
+                    "mean_evals": round(float(evals.mean()), 2),
+                    "entry_ms_mean": round(statistics.fmean(entry_ms), 4),
+                    "search_kernel_ms_mean": round(statistics.fmean(search_ms), 4)},
+            "arms": {"plain_fp32": plain, "fp32_from_entries": ent, "learned_bf16": lrn},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "kernel": "search_kernel (per launch = one step's 10,000 queries)",
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+                         "traffic_source": traffic_src,
+                         "step_achieved": round(alg_bytes / (statistics.fmean(kernel_ms) / 1000.0) / 1e9, 1),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
+                         else "fallback"},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(nq * w.dim * 4),
                     "d2h_bytes_per_step": int(nq * k * 8)},
-            "gpu_launches": args.steps * (1 + (0 if mode == "plain" or args.entries <= 0
-                                                else (2 if args.coarse > 0 else 1))),
+            "gpu_launches": args.steps * (1 + (0 if mode == "plain" or entries is None
+                                               else (5 if args.coarse > 0 else 1))),
             "clocks": clocks,
             "kernel_ms": {"min": round(min(kernel_ms), 4), "median": round(statistics.median(kernel_ms), 4),
                           "max": round(max(kernel_ms), 4)},
             "wall_s_timed": round(wall, 4),
         }
         print(json.dumps(line), flush=True)
-    if ixl is not None:
-        ixl.free()
-    if ent:
-        ixe.free()
-    ix32.free()
+    for a in arms.values():
+        a[1].free()
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if args.mode == "precision":
+        run_precision(args, torch, local)
+    elif args.mode == "serve":
+        run_serve(args, torch, local)
+    elif args.mode == "build":
+        run_build(args, torch, local)
+    else:
+        run_search(args, torch, rank, world, local, dist)
     if dist:
         dist.destroy_process_group()
 

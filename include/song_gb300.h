@@ -164,6 +164,16 @@ int song_index_set_early_exit(song_index *index, const float *weights, float thr
  * in the reference.  F32 and BF16 storage. */
 int song_index_set_hop_limit(song_index *index, int max_hops);
 
+/* Stage timing, the counterpart of the reference's __ENABLE_MEASURE stage
+ * timers (warp_astar_accelerator.h:32-38,358-408).  With enable != 0 every
+ * later search on the index records CUDA events on its launch stream around
+ * the entry-point choice and around the search kernel; song_index_timing
+ * waits for the last search's events and returns both stages in
+ * milliseconds (entry_ms 0 without entry points).  enable = 0 stops the
+ * recording; the events are released with the index. */
+int song_index_set_timing(song_index *index, int enable);
+int song_index_timing(song_index *index, float *entry_ms, float *search_ms);
+
 /* Entry points (warp_astar_accelerator.h:173 always starts at vertex 0, which
  * stays the default).  With count > 0 entry vertex ids, every query of
  * song_search, song_search_device and song_search_trace_device starts from

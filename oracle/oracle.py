@@ -89,6 +89,8 @@ def lib():
         L.orc_nearest_entry.argtypes = [P, P, i32, P, i32, i32, i32, P]
         L.orc_kernel_search_trace.restype = i32
         L.orc_kernel_search_trace.argtypes = [P, P, i32, i32, i32, i32, i32, P, P, P, P, P, P]
+        L.orc_graph_build.restype = i32
+        L.orc_graph_build.argtypes = [P, ctypes.c_uint64, i32, i32, i32, i32, i32, i32, i32, i32, P]
         L.orc_cpu_search.restype = i32
         L.orc_cpu_search.argtypes = [P, P, i32, i32, P, P, i32]
         L.orc_fixhash_hash.restype = i32
@@ -217,6 +219,19 @@ class OracleIndex:
         if rc != 0:
             raise ValueError("orc_cpu_search failed")
         return out, ex
+
+
+def graph_build(data, metric, shift=5, search_degree=15, fixed_degree=31, budget=150, batch_div=0, nthreads=None):
+    """The reference's CPU builder restated (orc_graph_build): the bfsg.graph
+    array (n << shift uint64)."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    n, dim = data.shape
+    out = np.empty(n << shift, dtype=np.uint64)
+    m = METRICS[metric] if isinstance(metric, str) else int(metric)
+    if lib().orc_graph_build(_ptr(data), n, dim, m, shift, search_degree, fixed_degree, budget, batch_div,
+                             nthreads or default_threads(), _ptr(out)) != 0:
+        raise ValueError("orc_graph_build failed")
+    return out
 
 
 def classify(log_a, log_b):

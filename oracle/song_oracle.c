@@ -1116,3 +1116,215 @@ done:
   free(members);
   return rc;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Graph builder: FixedDegreeGraph::add_vertex (graph.h:149-167)              */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  const float *data;
+  uint64_t n;
+  int dim, metric, shift, search_degree, fixed_degree;
+  uint64_t *edges;   /* n << shift: slot 0 = degree, then ids */
+  double *edge_dist; /* the distance of each edge, parallel to edges */
+} gbuild;
+
+static const float *gb_row(const gbuild *b, uint64_t i) { return b->data + i * (uint64_t)b->dim; }
+
+/* graph.h:98-114: Hoare partition around the middle element. */
+static void gb_qsort(gbuild *b, size_t l, size_t r) {
+  size_t mid = (l + r) >> 1;
+  long long i = (long long)l, j = (long long)r;
+  double k = b->edge_dist[mid];
+  do {
+    while (b->edge_dist[i] < k) ++i;
+    while (k < b->edge_dist[j]) --j;
+    if (i <= j) {
+      double td = b->edge_dist[i];
+      b->edge_dist[i] = b->edge_dist[j];
+      b->edge_dist[j] = td;
+      uint64_t te = b->edges[i];
+      b->edges[i] = b->edges[j];
+      b->edges[j] = te;
+      ++i;
+      --j;
+    }
+  } while (i <= j);
+  if ((size_t)i < r) gb_qsort(b, (size_t)i, r);
+  if (j >= 0 && l < (size_t)j) gb_qsort(b, l, (size_t)j);
+}
+
+/* graph.h:116-124: distances of a row's edges from its vertex, then sorted. */
+static void gb_rank_edges(gbuild *b, size_t off) {
+  const uint64_t deg = b->edges[off];
+  const float *a = gb_row(b, off >> b->shift);
+  for (uint64_t i = 0; i < deg; ++i)
+    b->edge_dist[off + i + 1] = orc_cpu_distance(b->metric, b->dim, a, gb_row(b, b->edges[off + i + 1]));
+  if (deg > 0) gb_qsort(b, off + 1, off + deg);
+}
+
+/* graph.h:32-55: a closer vertex replaces the farthest edge of a full row,
+ * then bubbles towards the front. */
+static void gb_rank_and_switch(gbuild *b, uint64_t v, uint64_t u) {
+  const double curr = orc_cpu_distance(b->metric, b->dim, gb_row(b, v), gb_row(b, u));
+  const size_t off = (size_t)v << b->shift;
+  const size_t last = off + b->edges[off];
+  if (curr >= b->edge_dist[last]) return;
+  b->edges[last] = u;
+  b->edge_dist[last] = curr;
+  for (size_t i = last - 1; i > off; --i) {
+    if (b->edge_dist[i] > b->edge_dist[i + 1]) {
+      double td = b->edge_dist[i];
+      b->edge_dist[i] = b->edge_dist[i + 1];
+      b->edge_dist[i + 1] = td;
+      uint64_t te = b->edges[i];
+      b->edges[i] = b->edges[i + 1];
+      b->edges[i + 1] = te;
+    } else {
+      break;
+    }
+  }
+}
+
+/* graph.h:126-137: append while the row has room (ranking it when it fills),
+ * afterwards replace the farthest edge if closer. */
+static void gb_add_edge(gbuild *b, uint64_t v, uint64_t u) {
+  const size_t off = (size_t)v << b->shift;
+  if (b->edges[off] < (uint64_t)b->fixed_degree) {
+    ++b->edges[off];
+    b->edges[off + b->edges[off]] = u;
+    if (b->edges[off] == (uint64_t)b->fixed_degree) gb_rank_edges(b, off);
+  } else {
+    gb_rank_and_switch(b, v, u);
+  }
+}
+
+/* graph.h:149-167 after the search: the search_degree nearest results become
+ * the vertex's edges (ranked), and each of them gets the reverse edge. */
+static void gb_apply(gbuild *b, uint64_t v, const uint64_t *nb, int cnt) {
+  const int num = cnt < b->search_degree ? cnt : b->search_degree;
+  const size_t off = (size_t)v << b->shift;
+  b->edges[off] = (uint64_t)num;
+  for (int i = 0; i < num; ++i) b->edges[off + i + 1] = nb[i];
+  gb_rank_edges(b, off);
+  for (int i = 0; i < num; ++i) gb_add_edge(b, nb[i], v);
+}
+
+typedef struct {
+  const gbuild *b;
+  orc_index ix;      /* the graph as it stands before the batch */
+  uint64_t a, e;     /* the batch */
+  int budget;
+  uint64_t *res;     /* (e - a) x budget result ids, ORC_NO_ID past the end */
+  volatile uint64_t next;
+  volatile int err;
+} gbatch;
+
+static void *gb_worker(void *arg) {
+  gbatch *j = (gbatch *)arg;
+  cscratch s;
+  memset(&s, 0, sizeof s);
+  s.t = (pr_t *)malloc(sizeof(pr_t) * (size_t)(j->budget + 2));
+  s.visited = (uint8_t *)calloc((size_t)j->b->n, 1);
+  if (!s.t || !s.visited) {
+    j->err = 1;
+  } else {
+    for (;;) {
+      const uint64_t v = __sync_fetch_and_add(&j->next, 1);
+      if (v >= j->e) break;
+      if (csearch_one(&j->ix, gb_row(j->b, v), j->budget, &s, j->res + (size_t)(v - j->a) * j->budget, NULL)) {
+        j->err = 1;
+        break;
+      }
+    }
+  }
+  free(s.q);
+  free(s.t);
+  free(s.visited);
+  free(s.touched);
+  return NULL;
+}
+
+int orc_graph_build(const float *data, uint64_t n, int dim, int metric, int shift, int search_degree,
+                    int fixed_degree, int budget, int batch_div, int nthreads, uint64_t *graph_out) {
+  if (!data || !graph_out || n == 0 || dim <= 0 || metric < ORC_L2 || metric > ORC_COS) return -1;
+  if (shift < 1 || shift > 10 || fixed_degree < 1 || fixed_degree > (1 << shift) - 1) return -1;
+  if (search_degree < 1 || search_degree > fixed_degree || budget < search_degree || batch_div < 0) return -1;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  gbuild b;
+  b.data = data;
+  b.n = n;
+  b.dim = dim;
+  b.metric = metric;
+  b.shift = shift;
+  b.search_degree = search_degree;
+  b.fixed_degree = fixed_degree;
+  b.edges = graph_out;
+  memset(graph_out, 0, sizeof(uint64_t) * ((size_t)n << shift));
+  b.edge_dist = (double *)calloc((size_t)n << shift, sizeof(double));
+  const uint64_t maxb = batch_div > 0 ? (n / (uint64_t)batch_div + 1) : 1;
+  uint64_t *res = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)maxb * (size_t)budget);
+  if (!b.edge_dist || !res) {
+    free(b.edge_dist);
+    free(res);
+    return -1;
+  }
+  int rc = 0;
+  uint64_t a = 0;
+  while (a < n && rc == 0) {
+    /* batch_div 0: one vertex at a time (the reference's loop); otherwise
+     * max(1, inserted / batch_div) vertices, searched against the graph as
+     * it stood before the batch and applied in id order */
+    uint64_t bs = batch_div > 0 ? a / (uint64_t)batch_div : 1;
+    if (bs < 1) bs = 1;
+    const uint64_t e = a + bs < n ? a + bs : n;
+    if (a == 0) {
+      /* data.h:139-144: the first vertex finds no other vertex */
+      for (uint64_t v = a; v < e; ++v) gb_apply(&b, v, res, 0);
+      a = e;
+      continue;
+    }
+    gbatch j;
+    memset(&j, 0, sizeof j);
+    j.b = &b;
+    j.ix.data = data;
+    j.ix.graph = graph_out;
+    j.ix.n = n;
+    j.ix.dim = dim;
+    j.ix.shift = shift;
+    j.ix.metric = metric;
+    j.a = a;
+    j.e = e;
+    j.budget = budget;
+    j.res = res;
+    j.next = a;
+    const uint64_t nt = e - a < (uint64_t)nthreads ? e - a : (uint64_t)nthreads;
+    if (nt <= 1) {
+      gb_worker(&j);
+    } else {
+      pthread_t th[256];
+      int started = 0;
+      for (uint64_t t = 0; t < nt; ++t) {
+        if (pthread_create(&th[t], NULL, gb_worker, &j) != 0) break;
+        ++started;
+      }
+      if (started == 0) gb_worker(&j);
+      for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    }
+    if (j.err) {
+      rc = -1;
+      break;
+    }
+    for (uint64_t v = a; v < e; ++v) {
+      const uint64_t *r = res + (size_t)(v - a) * budget;
+      int cnt = 0;
+      while (cnt < budget && r[cnt] != ORC_NO_ID) ++cnt;
+      gb_apply(&b, v, r, cnt);
+    }
+    a = e;
+  }
+  free(b.edge_dist);
+  free(res);
+  return rc;
+}

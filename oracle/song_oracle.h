@@ -140,6 +140,14 @@ int orc_classify(const orc_event *a, int na, const orc_event *b, int nb, int *at
 
 /* CPU best-first search of graph.h:169-216 with result size k.  out: nq x k
  * (ORC_NO_ID past the result length); explored may be NULL. */
+/* The reference's CPU graph builder (graph.h:149-167 with graph.h:32-55,
+ * 98-137): batch_div 0 inserts one vertex at a time (the reference's graph);
+ * batch_div > 0 inserts batches of max(1, inserted / batch_div) vertices,
+ * each searched against the graph before its batch on nthreads threads and
+ * applied in id order.  graph_out: n << shift uint64 (bfsg.graph layout). */
+int orc_graph_build(const float *data, uint64_t n, int dim, int metric, int shift, int search_degree,
+                    int fixed_degree, int budget, int batch_div, int nthreads, uint64_t *graph_out);
+
 int orc_cpu_search(const orc_index *ix, const float *queries, int nq, int k, uint64_t *out,
                    int32_t *explored, int nthreads);
 

@@ -43,7 +43,7 @@ EXPORTED = [
     "song_index_free", "song_index_info", "song_search", "song_search_device",
     "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_index_set_entries", "song_index_set_entries_2level", "song_debug_fixhash", "song_search_noalloc",
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
-    "song_index_set_hop_limit", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
+    "song_index_set_hop_limit", "song_index_set_timing", "song_index_timing", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
 ]
 MLP_PARAMS = 1281
@@ -111,6 +111,10 @@ def load_library():
     L.song_search_trace_device.argtypes = [P, P, i32, i32, i32, i32, P, P, P, P, P, P]
     L.song_index_set_hop_limit.restype = i32
     L.song_index_set_hop_limit.argtypes = [P, i32]
+    L.song_index_set_timing.restype = i32
+    L.song_index_set_timing.argtypes = [P, i32]
+    L.song_index_timing.restype = i32
+    L.song_index_timing.argtypes = [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     L.song_mlp_train_device.restype = i32
     L.song_mlp_train_device.argtypes = [P, P, P, ctypes.c_int64, P, i32, i32, ctypes.c_float, P, P, P]
     L.song_mlp_grad.restype = i32
@@ -239,6 +243,17 @@ class Index:
             return
         _check(L.song_index_set_entries(self._h, _ptr(e) if e is not None and e.size else None,
                                         0 if e is None else int(e.size), int(starts)))
+
+    def set_timing(self, enable=True):
+        """Record CUDA events around the entry choice and the search kernel of
+        every later search (song_index_set_timing)."""
+        _check(load_library().song_index_set_timing(self._h, int(bool(enable))))
+
+    def timing(self):
+        """(entry-choice ms, search-kernel ms) of the last search."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(load_library().song_index_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def set_hop_limit(self, max_hops):
         """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""

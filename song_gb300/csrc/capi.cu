@@ -93,6 +93,8 @@ void release(song_index *ix) {
   cudaFree(ix->d_cl_count);
   cudaFree(ix->d_entry_work);
   cudaFree(ix->d_starts);
+  for (cudaEvent_t &e : ix->ev)
+    if (e) cudaEventDestroy(e);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;
 }
@@ -110,12 +112,18 @@ int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_
   c.counter = ix->d_counter;
   c.error = ix->d_error;
   song::apply_index_settings(ix, c);
+  if (ix->timing) SONG_CUDA(cudaEventRecord(ix->ev[0], s));
   int rc = song::prepare_starts(ix, c, s);
   if (rc != SONG_OK) return rc;
   SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
+  if (ix->timing) {
+    SONG_CUDA(cudaEventRecord(ix->ev[1], s));
+    ix->timed_entries = c.starts != nullptr;
+  }
   int e = song::launch_search(ix->dx, c, s);
   if (e == -1) return fail(SONG_ERR_ARG, "unsupported search shape");
   if (e != 0) return fail(SONG_ERR_CUDA, "search launch: %s", cudaGetErrorString((cudaError_t)e));
+  if (ix->timing) SONG_CUDA(cudaEventRecord(ix->ev[2], s));
   return SONG_OK;
 }
 
@@ -454,6 +462,33 @@ int song_index_set_early_exit(song_index *ix, const float *weights, float thresh
   ix->exit_threshold = threshold;
   ix->exit_min_hops = min_hops;
   ix->exit_every = every;
+  return SONG_OK;
+}
+
+int song_index_set_timing(song_index *ix, int enable) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  if (enable)
+    for (cudaEvent_t &e : ix->ev)
+      if (!e) SONG_CUDA(cudaEventCreate(&e));
+  ix->timing = enable != 0;
+  ix->timed_entries = false;
+  return SONG_OK;
+}
+
+int song_index_timing(song_index *ix, float *entry_ms, float *search_ms) {
+  g_last_error.clear();
+  if (!ix || !ix->ev[2]) return fail(SONG_ERR_ARG, "timing is not enabled on this index");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  SONG_CUDA(cudaEventSynchronize(ix->ev[2]));
+  float a = 0.0f, b = 0.0f;
+  if (ix->timed_entries) SONG_CUDA(cudaEventElapsedTime(&a, ix->ev[0], ix->ev[1]));
+  SONG_CUDA(cudaEventElapsedTime(&b, ix->ev[1], ix->ev[2]));
+  if (entry_ms) *entry_ms = a;
+  if (search_ms) *search_ms = b;
   return SONG_OK;
 }
 

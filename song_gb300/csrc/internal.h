@@ -122,6 +122,11 @@ struct song_index {
   uint32_t *d_entry_work = nullptr;    // per-call lists of the two-level choice
   size_t cap_entry_work = 0;
   int servers = 0;  // servers using the entries (song_server_create); they stay fixed meanwhile
+  // stage timing (song_index_set_timing): events before the entry choice,
+  // before the search kernel, after it
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  bool timed_entries = false;
   uint32_t *d_starts = nullptr;
   size_t cap_starts = 0;
   uint64_t device_bytes = 0;

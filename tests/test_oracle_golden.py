@@ -162,3 +162,29 @@ def test_two_level_entry_choice_follows_its_definition(oracle):
     flat = ox.nearest_entry(q, ent, ns=4)
     for i in range(q.shape[0]):
         assert [int(x) for x in flat[i]] == [int(x) for x in nearest(q[i], list(ent), 4)]
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_oracle_builder_reproduces_reference_graph(oracle, name):
+    """orc_graph_build one vertex at a time is the reference's own builder:
+    the golden graphs were written by it."""
+    g = load_golden(name)
+    shift = int(g["shift"])
+    built = oracle.graph_build(g["data"], int(g["metric"]), shift, 7 if shift == 4 else 15, (1 << shift) - 1, 150,
+                               batch_div=0, nthreads=1)
+    assert np.array_equal(built, g["graph"])
+
+
+@pytest.mark.parametrize("name,n,div", [("scale-1m-128d-l2", 20000, 64), ("small-15k-16d-cos", 15000, 64),
+                                        ("precision-1m-960d-cos", 2000, 16)])
+def test_oracle_builder_batches_equal_the_product_builder(oracle, song, name, n, div):
+    """With batch_div > 0 the oracle's builder and the product's batch-parallel
+    builder agree bit for bit (the reference arm of the bench builds its graph
+    with the oracle, so both arms search the same graph)."""
+    from song_gb300 import datasets as D
+    w = D.WORKLOADS[name]
+    data = D.base_vectors(w, n=n)
+    args = (data, w.metric, w.shift, w.search_degree, w.fixed_degree, 150)
+    a = oracle.graph_build(*args, batch_div=div, nthreads=4)
+    b = song.graph_build(*args, batch_div=div, nthreads=4)
+    assert np.array_equal(a, b)
