@@ -253,6 +253,15 @@ int song_server_poll(song_server *server, uint64_t *tickets, int max, int *n_don
 int song_server_result(song_server *server, uint64_t ticket, uint64_t *out, int *nq, int *k);
 /* Drains published work, stops the kernel and frees the server. */
 int song_server_destroy(song_server *server);
+/* Warps that find no work for `polls` polls (~0.5 us apart; default 2^21,
+ * about a second) leave; the next submission relaunches the kernel.  Taken
+ * by the next launch. */
+int song_server_set_idle_polls(song_server *server, uint32_t polls);
+/* *running = 1 while the server's kernel has warps on the GPU. */
+int song_server_running(song_server *server, int *running);
+/* Waits up to timeout_ms for a request to complete: SONG_OK, or
+ * SONG_ERR_TIMEOUT if it has not completed by then (it stays queued). */
+int song_server_wait(song_server *server, uint64_t ticket, int timeout_ms);
 
 /* Size of the fixed device scratch array used by song_search_noalloc. */
 #define SONG_NOALLOC_SCRATCH_BYTES (16u << 20)
@@ -270,6 +279,18 @@ int song_server_destroy(song_server *server);
  * Calls overlapping on one GPU share the array and race: serialise them. */
 int song_search_noalloc(song_index *index, const float *queries, int nq, int pq, int k,
                         uint64_t *out);
+
+/* Test hooks for the failure paths (no counterpart in the reference).
+ * song_debug_fail_alloc(n): the n-th next device allocation of the library
+ * fails as out of memory (0: none).  song_debug_set_wait: the search kernel's
+ * bounded waits give up after wait_limit polls (default 2^24), and every
+ * batch of row copies expects extra_tx bytes (a multiple of 16) that no copy
+ * delivers -- a wait that cannot complete; the call then returns
+ * SONG_ERR_TIMEOUT and the index stays usable.  song_debug_server_hold(1):
+ * admitted requests are kept from the kernel until song_debug_server_hold(0). */
+int song_debug_fail_alloc(int n);
+int song_debug_set_wait(song_index *index, uint32_t wait_limit, uint32_t extra_tx);
+int song_debug_server_hold(song_server *server, int hold);
 
 /* The visited-hash slot function of the reference's default build
  * (fixhash.h:20-24) evaluated on the device for `count` ids, for tests. */

@@ -45,6 +45,8 @@ EXPORTED = [
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
     "song_index_set_hop_limit", "song_index_set_timing", "song_index_timing", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
+    "song_server_set_idle_polls", "song_server_running", "song_server_wait", "song_debug_fail_alloc",
+    "song_debug_set_wait", "song_debug_server_hold",
 ]
 MLP_PARAMS = 1281
 TRACE_FIELDS = 6
@@ -131,6 +133,18 @@ def load_library():
     L.song_server_result.argtypes = [P, ctypes.c_uint64, P, ctypes.POINTER(i32), ctypes.POINTER(i32)]
     L.song_server_destroy.restype = i32
     L.song_server_destroy.argtypes = [P]
+    L.song_server_set_idle_polls.restype = i32
+    L.song_server_set_idle_polls.argtypes = [P, ctypes.c_uint32]
+    L.song_server_running.restype = i32
+    L.song_server_running.argtypes = [P, ctypes.POINTER(i32)]
+    L.song_server_wait.restype = i32
+    L.song_server_wait.argtypes = [P, ctypes.c_uint64, i32]
+    L.song_debug_fail_alloc.restype = i32
+    L.song_debug_fail_alloc.argtypes = [i32]
+    L.song_debug_set_wait.restype = i32
+    L.song_debug_set_wait.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32]
+    L.song_debug_server_hold.restype = i32
+    L.song_debug_server_hold.argtypes = [P, i32]
     L.song_search_noalloc.restype = i32
     L.song_search_noalloc.argtypes = [P, P, i32, i32, i32, P]
     L.song_debug_fixhash.restype = i32
@@ -288,6 +302,12 @@ class Index:
                                                  ctypes.c_void_p(evals_ptr) if evals_ptr else None,
                                                  ctypes.c_void_p(stream) if stream else None))
 
+    def debug_set_wait(self, wait_limit=1 << 24, extra_tx=0):
+        """Test hook (song_debug_set_wait): the kernel's bounded waits give up
+        after wait_limit polls; extra_tx bytes that no copy delivers make a
+        wait that cannot complete."""
+        _check(load_library().song_debug_set_wait(self._h, int(wait_limit), int(extra_tx)))
+
     def free(self):
         if getattr(self, "_h", None) and self._h.value:
             load_library().song_index_free(self._h)
@@ -350,6 +370,11 @@ def graph_build_gpu(data, metric, shift=5, search_degree=15, fixed_degree=31, bu
                                                fixed_degree, budget, batch_div, device,
                                                nthreads or os.cpu_count() or 1, _ptr(out)))
     return out
+
+
+def debug_fail_alloc(n):
+    """Test hook: the n-th next device allocation of the library fails (0: none)."""
+    _check(load_library().song_debug_fail_alloc(int(n)))
 
 
 def debug_fixhash(ids, pq):

@@ -5,6 +5,7 @@
 #include <cuda_fp8.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +32,18 @@ int fail(int code, const char *fmt, ...) {
 }
 
 void clear_error() { g_last_error.clear(); }
+
+namespace {
+std::atomic<long long> g_fail_alloc{0};  // song_debug_fail_alloc: allocations left until one fails
+}  // namespace
+
+cudaError_t dev_malloc(void **p, size_t bytes) {
+  if (g_fail_alloc.load() > 0 && g_fail_alloc.fetch_sub(1) == 1) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
 
 int check_search_args(const song_index *ix, int nq, int pq, int k) {
   if (!ix) return fail(SONG_ERR_ARG, "null index");
@@ -69,7 +82,7 @@ int grow(T **p, size_t *cap, size_t need, uint64_t *acct) {
   *p = nullptr;
   *cap = 0;
   size_t n = need < 1024 ? 1024 : need;
-  SONG_CUDA(cudaMalloc(reinterpret_cast<void **>(p), n * sizeof(T)));
+  SONG_CUDA(song::dev_malloc(reinterpret_cast<void **>(p), n * sizeof(T)));
   *cap = n;
   *acct += n * sizeof(T);
   return SONG_OK;
@@ -173,6 +186,8 @@ void apply_index_settings(const song_index *ix, SearchCall &c) {
   c.exit_min_hops = ix->exit_min_hops;
   c.exit_every = ix->exit_every;
   c.exit_max_hops = ix->max_hops;
+  c.wait_limit = ix->wait_limit;
+  c.extra_tx = ix->extra_tx;
 }
 }  // namespace song
 
@@ -266,7 +281,7 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   } while (0)
   SONG_CUDA_IX(cudaStreamCreateWithFlags(&ix->stream, cudaStreamNonBlocking));
   const size_t f32_bytes = static_cast<size_t>(n) * dx.f32_row_bytes;
-  SONG_CUDA_IX(cudaMalloc(reinterpret_cast<void **>(&ix->d_rows_f32), f32_bytes));
+  SONG_CUDA_IX(song::dev_malloc(reinterpret_cast<void **>(&ix->d_rows_f32), f32_bytes));
   ix->device_bytes += f32_bytes;
   SONG_CUDA_IX(cudaMemsetAsync(ix->d_rows_f32, 0, f32_bytes, ix->stream));
   SONG_CUDA_IX(cudaMemcpy2DAsync(ix->d_rows_f32, dx.f32_row_bytes, data, sizeof(float) * dim,
@@ -276,7 +291,7 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   } else {
     // Low-precision rows for the search; the FP32 rows stay for the re-rank.
     const size_t rows_bytes = static_cast<size_t>(n) * dx.row_bytes;
-    SONG_CUDA_IX(cudaMalloc(&ix->d_rows, rows_bytes));
+    SONG_CUDA_IX(song::dev_malloc(&ix->d_rows, rows_bytes));
     ix->device_bytes += rows_bytes;
     const uint32_t in_floats = dx.f32_row_bytes / 4u;
     if (storage == SONG_STORAGE_BF16)
@@ -288,12 +303,12 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
                                                      dx.scale_off);
     SONG_CUDA_IX(cudaGetLastError());
   }
-  SONG_CUDA_IX(cudaMalloc(&ix->d_adj, slots * sizeof(uint32_t)));
+  SONG_CUDA_IX(song::dev_malloc(&ix->d_adj, slots * sizeof(uint32_t)));
   ix->device_bytes += slots * sizeof(uint32_t);
   SONG_CUDA_IX(cudaMemcpyAsync(ix->d_adj, adj.data(), slots * sizeof(uint32_t),
                                cudaMemcpyHostToDevice, ix->stream));
-  SONG_CUDA_IX(cudaMalloc(&ix->d_counter, 256));
-  SONG_CUDA_IX(cudaMalloc(&ix->d_error, 256));
+  SONG_CUDA_IX(song::dev_malloc(&ix->d_counter, 256));
+  SONG_CUDA_IX(song::dev_malloc(&ix->d_error, 256));
   ix->device_bytes += 512;
   SONG_CUDA_IX(cudaMemsetAsync(ix->d_error, 0, 256, ix->stream));
   SONG_CUDA_IX(cudaStreamSynchronize(ix->stream));
@@ -407,6 +422,23 @@ int song_astar_search_batch(const float *queries, int nq, int pq, uint64_t *resu
   return rc;
 }
 
+int song_debug_fail_alloc(int n) {
+  g_last_error.clear();
+  if (n < 0) return fail(SONG_ERR_ARG, "n must be >= 0");
+  song::g_fail_alloc.store(n);
+  return SONG_OK;
+}
+
+int song_debug_set_wait(song_index *ix, uint32_t wait_limit, uint32_t extra_tx) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (wait_limit < 1) return fail(SONG_ERR_ARG, "wait_limit must be >= 1");
+  if (extra_tx % 16 != 0 || extra_tx > (1u << 16)) return fail(SONG_ERR_ARG, "extra_tx must be a multiple of 16, <= 65536");
+  ix->wait_limit = wait_limit;
+  ix->extra_tx = extra_tx;
+  return SONG_OK;
+}
+
 int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_out) {
   g_last_error.clear();
   if (count < 0 || pq < 2 || pq > SONG_MAX_PQ || (count > 0 && (!ids || !slots_out)))
@@ -414,8 +446,8 @@ int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_ou
   if (count == 0) return SONG_OK;
   uint32_t *d_ids = nullptr;
   int32_t *d_out = nullptr;
-  SONG_CUDA(cudaMalloc(&d_ids, count * sizeof(uint32_t)));
-  cudaError_t e = cudaMalloc(&d_out, count * sizeof(int32_t));
+  SONG_CUDA(song::dev_malloc(&d_ids, count * sizeof(uint32_t)));
+  cudaError_t e = song::dev_malloc(&d_out, count * sizeof(int32_t));
   if (e == cudaSuccess)
     e = cudaMemcpy(d_ids, ids, count * sizeof(uint32_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
@@ -455,7 +487,7 @@ int song_index_set_early_exit(song_index *ix, const float *weights, float thresh
   std::vector<__nv_bfloat16> w(SONG_MLP_PARAMS);
   for (int i = 0; i < SONG_MLP_PARAMS; ++i) w[i] = __float2bfloat16_rn(weights[i]);
   if (!ix->d_mlp) {
-    SONG_CUDA(cudaMalloc(reinterpret_cast<void **>(&ix->d_mlp), sizeof(__nv_bfloat16) * SONG_MLP_PARAMS));
+    SONG_CUDA(song::dev_malloc(reinterpret_cast<void **>(&ix->d_mlp), sizeof(__nv_bfloat16) * SONG_MLP_PARAMS));
     ix->device_bytes += sizeof(__nv_bfloat16) * SONG_MLP_PARAMS;
   }
   SONG_CUDA(cudaMemcpy(ix->d_mlp, w.data(), sizeof(__nv_bfloat16) * SONG_MLP_PARAMS, cudaMemcpyHostToDevice));

@@ -18,6 +18,7 @@ constexpr uint64_t FH_R1 = 0xa0ab69ccd854fc0aULL;
 
 // Bounded waits: an mbarrier that does not complete within this many polls
 // (each poll may itself suspend in hardware) sets the error flag and returns.
+// The default of an index; song_debug_set_wait changes it per index.
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -65,8 +66,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Bounded wait for phase `parity` of `bar`; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < WAIT_LIMIT; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

@@ -627,7 +627,7 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
     cudaFree(ix->d_entry_work);
     ix->d_entry_work = nullptr;
     ix->cap_entry_work = 0;
-    cudaError_t e = cudaMalloc(&ix->d_entry_work, sizeof(uint32_t) * need);
+    cudaError_t e = song::dev_malloc(&ix->d_entry_work, sizeof(uint32_t) * need);
     if (e != cudaSuccess) return e;
     ix->cap_entry_work = need;
   }
@@ -721,7 +721,7 @@ int prepare_starts(song_index *ix, SearchCall &c, cudaStream_t s) {
     if (ix->d_starts) cudaFree(ix->d_starts);
     ix->d_starts = nullptr;
     ix->cap_starts = 0;
-    cudaError_t e = cudaMalloc(&ix->d_starts, sizeof(uint32_t) * need);
+    cudaError_t e = song::dev_malloc(&ix->d_starts, sizeof(uint32_t) * need);
     if (e != cudaSuccess) return fail(SONG_ERR_OOM, "entry starts: %s", cudaGetErrorString(e));
     ix->cap_starts = need;
   }
@@ -765,8 +765,8 @@ extern "C" int song_index_set_entries(song_index *ix, const uint64_t *ids, int c
   clear_entries(ix);
   if (count == 0) return SONG_OK;
   const int dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
-  e = cudaMalloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
-  if (e == cudaSuccess) e = cudaMalloc(&ix->d_entry_rows, sizeof(float) * count * static_cast<size_t>(dpad));
+  e = song::dev_malloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_entry_rows, sizeof(float) * count * static_cast<size_t>(dpad));
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(ix->d_entry_ids, h.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess) {
@@ -827,9 +827,9 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
   uint32_t *d_ids = nullptr, *d_assign = nullptr, *d_perm = nullptr;
   float *d_rows = nullptr;
   std::vector<uint32_t> assign(static_cast<size_t>(count - coarse));
-  e = cudaMalloc(&d_ids, sizeof(uint32_t) * count);
-  if (e == cudaSuccess) e = cudaMalloc(&d_rows, sizeof(float) * static_cast<size_t>(count) * dpad);
-  if (e == cudaSuccess && count > coarse) e = cudaMalloc(&d_assign, sizeof(uint32_t) * (count - coarse));
+  e = song::dev_malloc(&d_ids, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = song::dev_malloc(&d_rows, sizeof(float) * static_cast<size_t>(count) * dpad);
+  if (e == cudaSuccess && count > coarse) e = song::dev_malloc(&d_assign, sizeof(uint32_t) * (count - coarse));
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_ids, h.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess) {
     gather_entry_rows_kernel<<<256, 256, 0, ix->stream>>>(ix->dx.rows_f32, static_cast<uint32_t>(dpad), d_ids, count,
@@ -877,12 +877,12 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
   for (int k = 0; k < coarse; ++k) cperm[k] = static_cast<uint32_t>(corder[k]);
   // 3. device copies: entries in cluster order, coarse rows by id, offsets
   uint32_t *d_cperm = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc(&d_perm, sizeof(uint32_t) * count);
-  if (e == cudaSuccess) e = cudaMalloc(&d_cperm, sizeof(uint32_t) * coarse);
-  if (e == cudaSuccess) e = cudaMalloc(&ix->d_entry_rows, sizeof(float) * static_cast<size_t>(count) * dpad);
-  if (e == cudaSuccess) e = cudaMalloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
-  if (e == cudaSuccess) e = cudaMalloc(&ix->d_coarse_rows, sizeof(float) * static_cast<size_t>(coarse) * dpad);
-  if (e == cudaSuccess) e = cudaMalloc(&ix->d_offsets, sizeof(uint32_t) * (coarse + 1));
+  if (e == cudaSuccess) e = song::dev_malloc(&d_perm, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = song::dev_malloc(&d_cperm, sizeof(uint32_t) * coarse);
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_entry_rows, sizeof(float) * static_cast<size_t>(count) * dpad);
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_coarse_rows, sizeof(float) * static_cast<size_t>(coarse) * dpad);
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_offsets, sizeof(uint32_t) * (coarse + 1));
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_perm, perm.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_cperm, cperm.data(), sizeof(uint32_t) * coarse, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess)
@@ -898,7 +898,7 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
     e = cudaGetLastError();
   }
   // 4. the per-cluster probe counters of the second kernel
-  if (e == cudaSuccess) e = cudaMalloc(&ix->d_cl_count, sizeof(uint32_t) * coarse);
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_cl_count, sizeof(uint32_t) * coarse);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
   cudaFree(d_ids);
   cudaFree(d_rows);

@@ -394,13 +394,13 @@ extern "C" int song_graph_build_gpu(const float *data, uint64_t n, int dim, int 
       return fail(e_ == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, \
                   "graph build: %s: %s", #call, cudaGetErrorString(e_));          \
   } while (0)
-  SONG_GB_CK(cudaMalloc(&d_data.p, sizeof(float) * n * dim));
-  SONG_GB_CK(cudaMalloc(&d_adj.p, sizeof(uint32_t) * (n << shift)));
-  SONG_GB_CK(cudaMalloc(&d_out.p, sizeof(uint32_t) * max_batch * search_degree));
-  SONG_GB_CK(cudaMalloc(&d_cnt.p, sizeof(int32_t) * max_batch));
-  SONG_GB_CK(cudaMalloc(&d_ctl.p, 256));
-  SONG_GB_CK(cudaMalloc(&d_rows.p, sizeof(uint32_t) * rows_cap * w));
-  SONG_GB_CK(cudaMalloc(&d_ids.p, sizeof(uint64_t) * rows_cap));
+  SONG_GB_CK(song::dev_malloc(&d_data.p, sizeof(float) * n * dim));
+  SONG_GB_CK(song::dev_malloc(&d_adj.p, sizeof(uint32_t) * (n << shift)));
+  SONG_GB_CK(song::dev_malloc(&d_out.p, sizeof(uint32_t) * max_batch * search_degree));
+  SONG_GB_CK(song::dev_malloc(&d_cnt.p, sizeof(int32_t) * max_batch));
+  SONG_GB_CK(song::dev_malloc(&d_ctl.p, 256));
+  SONG_GB_CK(song::dev_malloc(&d_rows.p, sizeof(uint32_t) * rows_cap * w));
+  SONG_GB_CK(song::dev_malloc(&d_ids.p, sizeof(uint64_t) * rows_cap));
   SONG_GB_CK(cudaMallocHost(&h_out.p, sizeof(uint32_t) * max_batch * search_degree));
   SONG_GB_CK(cudaMallocHost(&h_cnt.p, sizeof(int32_t) * max_batch));
   SONG_GB_CK(cudaMallocHost(&h_err.p, 256));
@@ -409,7 +409,7 @@ extern "C" int song_graph_build_gpu(const float *data, uint64_t n, int dim, int 
   SONG_GB_CK(cudaMemcpyAsync(d_data.p, data, sizeof(float) * n * dim, cudaMemcpyHostToDevice, st));
   SONG_GB_CK(cudaMemsetAsync(d_adj.p, 0, sizeof(uint32_t) * (n << shift), st));
   if (metric == SONG_METRIC_COS) {
-    SONG_GB_CK(cudaMalloc(&d_norms.p, sizeof(float) * n));
+    SONG_GB_CK(song::dev_malloc(&d_norms.p, sizeof(float) * n));
     row_norms_kernel<<<sms * 8, 256, 0, st>>>(static_cast<const float *>(d_data.p), n, dim,
                                               static_cast<float *>(d_norms.p));
     SONG_GB_CK(cudaGetLastError());
@@ -419,8 +419,8 @@ extern "C" int song_graph_build_gpu(const float *data, uint64_t n, int dim, int 
     if (d_vis.p) cudaFree(d_vis.p);
     if (d_q.p) cudaFree(d_q.p);
     d_vis.p = d_q.p = nullptr;
-    cudaError_t e1 = cudaMalloc(&d_vis.p, sizeof(uint32_t) * (warps << vis_log2));
-    if (e1 == cudaSuccess) e1 = cudaMalloc(&d_q.p, sizeof(QE) * (warps << q_log2));
+    cudaError_t e1 = song::dev_malloc(&d_vis.p, sizeof(uint32_t) * (warps << vis_log2));
+    if (e1 == cudaSuccess) e1 = song::dev_malloc(&d_q.p, sizeof(QE) * (warps << q_log2));
     if (e1 != cudaSuccess)
       return fail(e1 == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "graph build: scratch: %s",
                   cudaGetErrorString(e1));

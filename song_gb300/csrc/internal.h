@@ -44,6 +44,8 @@ struct SearchCall {
   int32_t *trace_final = nullptr;  // nq x 2: final top-k version, hops traced
   const uint32_t *starts = nullptr;  // nq x n_starts start vertices (entry points), null = vertex 0
   int n_starts = 1;
+  uint32_t wait_limit = 1u << 24;  // polls of a bounded mbarrier wait
+  uint32_t extra_tx = 0;           // test hook (song_debug_set_wait)
 };
 
 // Launch the plain search.  Returns a cudaError_t-compatible code (0 ok) or
@@ -74,6 +76,14 @@ struct DeviceGuard {
   }
 };
 
+// Device allocations of the library go through here, so that a test can make
+// one fail (song_debug_fail_alloc).
+cudaError_t dev_malloc(void **p, size_t bytes);
+template <class T>
+cudaError_t dev_malloc(T **p, size_t bytes) {
+  return dev_malloc(reinterpret_cast<void **>(p), bytes);
+}
+
 // Error reporting of the C ABI (capi.cu): records the message for
 // song_last_error() on the calling thread and returns `code`.
 int fail(int code, const char *fmt, ...);
@@ -96,6 +106,8 @@ struct song_index {
   int exit_min_hops = 0;
   int exit_every = 1;
   int max_hops = 0;                 // fixed hop budget, 0 = off
+  uint32_t wait_limit = 1u << 24;   // polls of the kernel's bounded waits (song_debug_set_wait)
+  uint32_t extra_tx = 0;            // test hook: bytes no copy delivers (song_debug_set_wait)
   uint32_t *d_counter = nullptr;
   int32_t *d_error = nullptr;
   cudaStream_t stream = nullptr;

@@ -177,11 +177,11 @@ int song_mlp_train_device(const float *d_x, const float *d_y, const float *d_w, 
   const int64_t nwarps = (static_cast<int64_t>(batch) + song::CHUNK - 1) / song::CHUNK;
   float *partial = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr, *lossbuf = nullptr;
   const int64_t steps = (n + batch - 1) / batch;
-  cudaError_t e = cudaMalloc(&partial, sizeof(float) * nwarps * song::PARTIAL);
-  if (e == cudaSuccess) e = cudaMalloc(&grad, sizeof(float) * MLP_NPARAM);
-  if (e == cudaSuccess) e = cudaMalloc(&m, sizeof(float) * MLP_NPARAM);
-  if (e == cudaSuccess) e = cudaMalloc(&v, sizeof(float) * MLP_NPARAM);
-  if (e == cudaSuccess) e = cudaMalloc(&lossbuf, sizeof(float) * steps);
+  cudaError_t e = song::dev_malloc(&partial, sizeof(float) * nwarps * song::PARTIAL);
+  if (e == cudaSuccess) e = song::dev_malloc(&grad, sizeof(float) * MLP_NPARAM);
+  if (e == cudaSuccess) e = song::dev_malloc(&m, sizeof(float) * MLP_NPARAM);
+  if (e == cudaSuccess) e = song::dev_malloc(&v, sizeof(float) * MLP_NPARAM);
+  if (e == cudaSuccess) e = song::dev_malloc(&lossbuf, sizeof(float) * steps);
   if (e == cudaSuccess) e = cudaMemsetAsync(m, 0, sizeof(float) * MLP_NPARAM, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, sizeof(float) * MLP_NPARAM, s);
   int rc = SONG_OK;
@@ -234,13 +234,13 @@ int song_mlp_grad(const float *x, const float *y, const float *w, int n, const f
   const int64_t nwarps = (static_cast<int64_t>(n) + song::CHUNK - 1) / song::CHUNK;
   float *dx = nullptr, *dy = nullptr, *dw = nullptr, *dp = nullptr, *partial = nullptr, *grad = nullptr,
         *loss = nullptr;
-  cudaError_t e = cudaMalloc(&dx, sizeof(float) * n * song::MLP_IN);
-  if (e == cudaSuccess) e = cudaMalloc(&dy, sizeof(float) * n);
-  if (e == cudaSuccess && w) e = cudaMalloc(&dw, sizeof(float) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(float) * MLP_NPARAM);
-  if (e == cudaSuccess) e = cudaMalloc(&partial, sizeof(float) * nwarps * song::PARTIAL);
-  if (e == cudaSuccess) e = cudaMalloc(&grad, sizeof(float) * MLP_NPARAM);
-  if (e == cudaSuccess) e = cudaMalloc(&loss, sizeof(float));
+  cudaError_t e = song::dev_malloc(&dx, sizeof(float) * n * song::MLP_IN);
+  if (e == cudaSuccess) e = song::dev_malloc(&dy, sizeof(float) * n);
+  if (e == cudaSuccess && w) e = song::dev_malloc(&dw, sizeof(float) * n);
+  if (e == cudaSuccess) e = song::dev_malloc(&dp, sizeof(float) * MLP_NPARAM);
+  if (e == cudaSuccess) e = song::dev_malloc(&partial, sizeof(float) * nwarps * song::PARTIAL);
+  if (e == cudaSuccess) e = song::dev_malloc(&grad, sizeof(float) * MLP_NPARAM);
+  if (e == cudaSuccess) e = song::dev_malloc(&loss, sizeof(float));
   if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(float) * n * song::MLP_IN, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dy, y, sizeof(float) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && w) e = cudaMemcpy(dw, w, sizeof(float) * n, cudaMemcpyHostToDevice);
@@ -266,9 +266,9 @@ int song_mlp_forward(const float *x, int n, const float *params, float *logits_o
   song::clear_error();
   if (!x || !params || !logits_out || n < 1) return song::fail(SONG_ERR_ARG, "bad arguments");
   float *dx = nullptr, *dp = nullptr, *dl = nullptr;
-  cudaError_t e = cudaMalloc(&dx, sizeof(float) * n * song::MLP_IN);
-  if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(float) * MLP_NPARAM);
-  if (e == cudaSuccess) e = cudaMalloc(&dl, sizeof(float) * n);
+  cudaError_t e = song::dev_malloc(&dx, sizeof(float) * n * song::MLP_IN);
+  if (e == cudaSuccess) e = song::dev_malloc(&dp, sizeof(float) * MLP_NPARAM);
+  if (e == cudaSuccess) e = song::dev_malloc(&dl, sizeof(float) * n);
   if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(float) * n * song::MLP_IN, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dp, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {

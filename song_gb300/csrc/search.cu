@@ -165,6 +165,8 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
   p.trace_final = c.trace_final;
   p.starts = c.starts;
   p.n_starts = c.starts ? c.n_starts : 1;
+  p.wait_limit = c.wait_limit;
+  p.extra_tx = c.extra_tx;
   if (learned) {
     if (ix.storage == 2) return -1;
     return launch_learned(p, ix.storage, ix.metric, L.H, L.S, stream);

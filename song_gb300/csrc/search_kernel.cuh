@@ -74,6 +74,8 @@ struct Params {
   int cap;
   uint64_t magic;  // VisitedHash (plain kernel)
   int log2cap;     // ExactVisited (learned kernel)
+  uint32_t wait_limit;  // polls of a bounded mbarrier wait
+  uint32_t extra_tx;    // test hook: bytes every copy batch expects beyond its rows (0 in use)
   // learned variant
   const __nv_bfloat16 *mlp;  // MLP_NPARAM weights (BF16), null = no early exit
   float exit_threshold;
@@ -138,7 +140,7 @@ __device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage
     // The buffer was last read through the generic proxy; order those reads
     // before the async-proxy writes of the copies issued below.
     fence_proxy_async();
-    if (lane == 0) mbar_arrive_expect_tx(&mbar[b], static_cast<uint32_t>(cnt) * rb);
+    if (lane == 0) mbar_arrive_expect_tx(&mbar[b], static_cast<uint32_t>(cnt) * rb + p.extra_tx);
     __syncwarp();
     const uint32_t id = __shfl_sync(FULL, cid, (first + lane) & 31);
     if (lane < cnt)
@@ -151,7 +153,12 @@ __device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage
   for (int c = 0; c < nchunks; ++c) {
     const int b = c & 1;
     uint32_t &ph = b ? ph1 : ph0;
-    if (!mbar_wait(&mbar[b], ph)) return false;
+    if (!mbar_wait(&mbar[b], ph, p.wait_limit)) {
+      // give up: wait (bounded again) for the other buffer's copies, still in
+      // flight into this warp's shared memory, before the warp leaves
+      if (c + 1 < nchunks) mbar_wait(&mbar[b ^ 1], b ? ph0 : ph1, p.wait_limit);
+      return false;
+    }
     ph ^= 1u;
     const int first = c * H;
     const int cnt = min(H, m - first);

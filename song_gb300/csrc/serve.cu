@@ -13,9 +13,11 @@
 // (zero-copy); a per-slot completion counter is bumped after each query with
 // system-scope release ordering, and the host polls it.
 //
-// Waits are bounded: a warp that finds no work for SERVE_IDLE_POLLS polls exits
-// (an idle exit, not an error); when every warp has exited the host relaunches
-// the kernel on the next submission.  Warps claim an entry only after it is
+// Waits are bounded: a warp that finds no work for `idle_polls` polls (about
+// a second by default; song_server_set_idle_polls) exits (an idle exit, not
+// an error); when every warp has exited the host relaunches the kernel on the
+// next submission.  The host's own wait for a request, song_server_wait, is
+// bounded too and returns SONG_ERR_TIMEOUT.  Warps claim an entry only after it is
 // published, so an exiting warp never holds unprocessed work.
 #include <cuda_runtime.h>
 
@@ -25,6 +27,7 @@
 #include <cstring>
 #include <deque>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -35,7 +38,7 @@
 namespace song {
 namespace {
 
-constexpr uint32_t SERVE_IDLE_POLLS = 1u << 21;  // x ~0.5 us backoff: about a second idle
+constexpr uint32_t SERVE_IDLE_POLLS = 1u << 21;  // default; x ~0.5 us backoff: about a second idle
 
 struct ServeEntry {
   uint64_t query;    // device-visible address of the query vector
@@ -122,7 +125,7 @@ __device__ __forceinline__ void serve_choose_starts(const Params &p, const float
 template <int METRIC, int STORAGE, int H, int S>
 __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1)
     serve_kernel(const Params p, const ServeEntry *ring, uint32_t ring_mask, const ServeCtl *ctl,
-                 uint32_t *next, uint32_t *done) {
+                 uint32_t *next, uint32_t *done, uint32_t idle_polls) {
   extern __shared__ __align__(128) uint8_t smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -161,7 +164,7 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1)
           state = 2;
           break;
         }
-        if (polls >= SERVE_IDLE_POLLS) {
+        if (polls >= idle_polls) {
           state = 3;
           break;
         }
@@ -204,7 +207,7 @@ uint32_t align_up(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
 template <int METRIC, int STORAGE, int H, int S>
 cudaError_t launch_serve(const Params &p, const ServeEntry *ring, uint32_t mask, const ServeCtl *ctl,
-                         uint32_t *next, uint32_t *done, float fraction, cudaStream_t s) {
+                         uint32_t *next, uint32_t *done, float fraction, uint32_t idle, cudaStream_t s) {
   auto kern = serve_kernel<METRIC, STORAGE, H, S>;
   int wpb = 0, cap = 0;
   int e = get_shape(reinterpret_cast<const void *>(kern), p.warp_bytes, 0u, &wpb, &cap);
@@ -212,32 +215,33 @@ cudaError_t launch_serve(const Params &p, const ServeEntry *ring, uint32_t mask,
   int grid = static_cast<int>(fraction * cap + 0.5f);
   if (grid < 1) grid = 1;
   if (grid > cap) grid = cap;
-  kern<<<grid, wpb * 32, static_cast<size_t>(p.warp_bytes) * wpb, s>>>(p, ring, mask, ctl, next, done);
+  kern<<<grid, wpb * 32, static_cast<size_t>(p.warp_bytes) * wpb, s>>>(p, ring, mask, ctl, next, done, idle);
   return cudaGetLastError();
 }
 
 template <int METRIC, int H>
 cudaError_t launch_serve_s(int S, const Params &p, const ServeEntry *ring, uint32_t mask, const ServeCtl *ctl,
-                           uint32_t *next, uint32_t *done, float f, cudaStream_t s) {
+                           uint32_t *next, uint32_t *done, float f, uint32_t idle, cudaStream_t s) {
   switch (S) {
     case 1:
     case 2:
-    case 4: return launch_serve<METRIC, 0, H, 4>(p, ring, mask, ctl, next, done, f, s);
-    case 8: return launch_serve<METRIC, 0, H, 8>(p, ring, mask, ctl, next, done, f, s);
-    case 16: return launch_serve<METRIC, 0, H, 16>(p, ring, mask, ctl, next, done, f, s);
-    default: return launch_serve<METRIC, 0, H, 32>(p, ring, mask, ctl, next, done, f, s);
+    case 4: return launch_serve<METRIC, 0, H, 4>(p, ring, mask, ctl, next, done, f, idle, s);
+    case 8: return launch_serve<METRIC, 0, H, 8>(p, ring, mask, ctl, next, done, f, idle, s);
+    case 16: return launch_serve<METRIC, 0, H, 16>(p, ring, mask, ctl, next, done, f, idle, s);
+    default: return launch_serve<METRIC, 0, H, 32>(p, ring, mask, ctl, next, done, f, idle, s);
   }
 }
 
 cudaError_t launch_serve_any(int metric, int H, int S, const Params &p, const ServeEntry *ring, uint32_t mask,
-                             const ServeCtl *ctl, uint32_t *next, uint32_t *done, float f, cudaStream_t s) {
+                             const ServeCtl *ctl, uint32_t *next, uint32_t *done, float f, uint32_t idle,
+                             cudaStream_t s) {
   switch (metric * 2 + (H == 4 ? 1 : 0)) {
-    case 0: return launch_serve_s<0, 2>(S, p, ring, mask, ctl, next, done, f, s);
-    case 1: return launch_serve_s<0, 4>(S, p, ring, mask, ctl, next, done, f, s);
-    case 2: return launch_serve_s<1, 2>(S, p, ring, mask, ctl, next, done, f, s);
-    case 3: return launch_serve_s<1, 4>(S, p, ring, mask, ctl, next, done, f, s);
-    case 4: return launch_serve_s<2, 2>(S, p, ring, mask, ctl, next, done, f, s);
-    default: return launch_serve_s<2, 4>(S, p, ring, mask, ctl, next, done, f, s);
+    case 0: return launch_serve_s<0, 2>(S, p, ring, mask, ctl, next, done, f, idle, s);
+    case 1: return launch_serve_s<0, 4>(S, p, ring, mask, ctl, next, done, f, idle, s);
+    case 2: return launch_serve_s<1, 2>(S, p, ring, mask, ctl, next, done, f, idle, s);
+    case 3: return launch_serve_s<1, 4>(S, p, ring, mask, ctl, next, done, f, idle, s);
+    case 4: return launch_serve_s<2, 2>(S, p, ring, mask, ctl, next, done, f, idle, s);
+    default: return launch_serve_s<2, 4>(S, p, ring, mask, ctl, next, done, f, idle, s);
   }
 }
 
@@ -277,6 +281,8 @@ struct song_server {
   uint32_t published = 0;
   bool running = false;
   bool holds_entries = false;  // counted in ix->servers: the index's entries stay fixed
+  uint32_t idle_polls = song::SERVE_IDLE_POLLS;
+  bool hold = false;           // test hook: admitted requests are not published while set
   uint64_t next_ticket = 1;
   std::vector<Slot> slots;
   std::deque<Pending> pending;
@@ -298,7 +304,7 @@ int relaunch_if_idle(song_server *s) {
   // Every warp has left and none holds a claim, so the claim counter already
   // counts exactly the processed entries: the new launch continues from it.
   cudaError_t e = song::launch_serve_any(s->ix->dx.metric, s->H, s->S, s->params, s->d_ring, s->ring_mask, s->d_ctl,
-                               s->d_next, s->d_done, s->fraction, s->stream);
+                                         s->d_next, s->d_done, s->fraction, s->idle_polls, s->stream);
   if (e != cudaSuccess) return fail(SONG_ERR_CUDA, "serve launch: %s", cudaGetErrorString(e));
   s->running = true;
   return SONG_OK;
@@ -325,6 +331,7 @@ void admit(song_server *s, int slot_i, song_server::Pending &r) {
     e.k = static_cast<uint16_t>(r.k);
   }
   s->published += static_cast<uint32_t>(r.nq);
+  if (s->hold) return;  // the entries wait in the ring until the hold is released
   std::atomic_thread_fence(std::memory_order_release);
   __atomic_store_n(&s->h_ctl->published, s->published, __ATOMIC_RELEASE);
 }
@@ -387,7 +394,7 @@ int song_server_create(song_index *ix, int max_pq, int max_k, int nslots, int sl
   if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_ring), s->h_ring, 0);
   if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_ctl), s->h_ctl, 0);
   if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_done), s->h_done, 0);
-  if (e == cudaSuccess) e = cudaMalloc(&s->d_next, 256);
+  if (e == cudaSuccess) e = song::dev_malloc(&s->d_next, 256);
   if (e == cudaSuccess) e = cudaMemsetAsync(s->d_next, 0, 256, s->stream);
   if (e != cudaSuccess) {
     int rc = fail(e == cudaErrorMemoryAllocation ? SONG_ERR_OOM : SONG_ERR_CUDA, "server create: %s",
@@ -412,6 +419,8 @@ int song_server_create(song_index *ix, int max_pq, int max_k, int nslots, int sl
   p.shift = dx.shift;
   p.dim = dim;
   p.error = ix->d_error;
+  p.wait_limit = ix->wait_limit;
+  p.extra_tx = ix->extra_tx;
   p.n_starts = 1;
   if (ix->n_entries > 0) {  // the index's entry points, fixed for the server's life
     p.entry_rows = ix->d_entry_rows;
@@ -539,6 +548,78 @@ int song_server_result(song_server *s, uint64_t ticket, uint64_t *out, int *nq, 
     }
   }
   return fail(SONG_ERR_ARG, "unknown request %llu", (unsigned long long)ticket);
+}
+
+int song_server_set_idle_polls(song_server *s, uint32_t polls) {
+  song::clear_error();
+  if (!s || polls < 1) return fail(SONG_ERR_ARG, "null server or polls < 1");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->idle_polls = polls;  // taken by the next launch
+  return SONG_OK;
+}
+
+int song_server_running(song_server *s, int *running) {
+  song::clear_error();
+  if (!s || !running) return fail(SONG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->running) {
+    const cudaError_t q = cudaStreamQuery(s->stream);
+    if (q == cudaSuccess) s->running = false;
+    else if (q != cudaErrorNotReady) return fail(SONG_ERR_CUDA, "serve kernel: %s", cudaGetErrorString(q));
+  }
+  *running = s->running ? 1 : 0;
+  return SONG_OK;
+}
+
+int song_server_wait(song_server *s, uint64_t ticket, int timeout_ms) {
+  song::clear_error();
+  if (!s || timeout_ms < 0) return fail(SONG_ERR_ARG, "null server or negative timeout");
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      int found = -1;
+      for (int i = 0; i < s->nslots; ++i)
+        if (s->slots[i].busy && s->slots[i].ticket == ticket) found = i;
+      bool queued = false;
+      for (const auto &r : s->pending) queued = queued || r.ticket == ticket;
+      if (found < 0 && !queued) return fail(SONG_ERR_ARG, "unknown request %llu", (unsigned long long)ticket);
+      if (found >= 0 && s->slots[found].complete) return SONG_OK;
+      if (found >= 0 && __atomic_load_n(&s->h_done[found], __ATOMIC_ACQUIRE) >=
+                            static_cast<uint32_t>(s->slots[found].nq)) {
+        s->slots[found].complete = true;  // as song_server_poll marks it; poll reports it too
+        s->completed.push_back(ticket);
+        return SONG_OK;
+      }
+      int prev = -1;
+      cudaGetDevice(&prev);
+      if (prev != s->ix->device) cudaSetDevice(s->ix->device);
+      const int rc = s->hold ? SONG_OK : relaunch_if_idle(s);
+      if (prev >= 0 && prev != s->ix->device) cudaSetDevice(prev);
+      if (rc) return rc;
+    }
+    const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0);
+    if (ms.count() >= timeout_ms)
+      return fail(SONG_ERR_TIMEOUT, "request %llu not complete after %d ms", (unsigned long long)ticket, timeout_ms);
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+int song_debug_server_hold(song_server *s, int hold) {
+  song::clear_error();
+  if (!s) return fail(SONG_ERR_ARG, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->hold = hold != 0;
+  if (s->hold) return SONG_OK;
+  // release: publish what was admitted meanwhile and make sure warps run
+  std::atomic_thread_fence(std::memory_order_release);
+  __atomic_store_n(&s->h_ctl->published, s->published, __ATOMIC_RELEASE);
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != s->ix->device) cudaSetDevice(s->ix->device);
+  const int rc = relaunch_if_idle(s);
+  if (prev >= 0 && prev != s->ix->device) cudaSetDevice(prev);
+  return rc;
 }
 
 int song_server_destroy(song_server *s) {

@@ -38,6 +38,25 @@ class Server:
         assert a.value == nq and b.value == k
         return out
 
+    def set_idle_polls(self, polls):
+        """Warps leave after `polls` idle polls (~0.5 us each); the next
+        submission relaunches them."""
+        _check(load_library().song_server_set_idle_polls(self._h, int(polls)))
+
+    def running(self):
+        r = ctypes.c_int()
+        _check(load_library().song_server_running(self._h, ctypes.byref(r)))
+        return bool(r.value)
+
+    def wait(self, ticket, timeout_ms):
+        """Waits for a request (SongError with status SONG_ERR_TIMEOUT if it
+        has not completed within timeout_ms)."""
+        _check(load_library().song_server_wait(self._h, ctypes.c_uint64(ticket), int(timeout_ms)))
+
+    def hold(self, on=True):
+        """Test hook: keep admitted requests from the kernel until released."""
+        _check(load_library().song_debug_server_hold(self._h, int(bool(on))))
+
     def close(self):
         if self._h and self._h.value:
             load_library().song_server_destroy(self._h)
