@@ -36,3 +36,18 @@ def test_noalloc_rejects_batches_beyond_its_scratch(song):
         with pytest.raises(song.SongError) as e:
             ix.search_noalloc(q, 100, 100)
         assert e.value.status == song.SONG_ERR_ARG and "scratch" in str(e.value)
+
+
+def test_noalloc_starts_at_vertex_0_whatever_the_entry_points(song):
+    """Entry points set on the index are not used: the ids are song_search's
+    with the entries cleared."""
+    g = load_golden("l2_s5_d32")
+    with song.Index(g["graph"], g["data"], int(g["shift"]), int(g["metric"])) as ix:
+        q = g["queries"]
+        plain = ix.search(q, 50, 10)
+        ix.set_entries(song.sample_entries(ix.n, 64, seed=3), starts=2)
+        try:
+            assert np.array_equal(ix.search_noalloc(q, 50, 10), plain)
+            assert np.array_equal(ix.search_noalloc(q, 50, 10), plain)
+        finally:
+            ix.set_entries(None)
