@@ -88,7 +88,8 @@ def parse_args():
                    help="best: measure the plain FP32 search (from vertex 0, the reference's semantics), the "
                         "same search from the nearest of --entries sampled entry vertices, and the learned "
                         "early exit + BF16 (+FP32 rerank), and report the fastest at the recall target; "
-                        "learned / plain / entries: that path only; "
+                        "plain / entries: that path only; learned: the early-exit study (vs the search "
+                        "without it and a fixed hop budget, from vertex 0 and from entry points); "
                         "precision: storage error and recall table; serve: Poisson request stream; "
                         "build: graph construction, GPU searches vs the CPU builder")
     p.add_argument("--entries", type=int, default=262144, help="entry vertices of the entries arm (sampled, seeded)")
@@ -100,11 +101,13 @@ def parse_args():
     p.add_argument("--serve-seconds", type=float, default=6.0, help="length of each request stream (serve)")
     p.add_argument("--rerank", type=int, default=100, help="FP32 re-ranked candidates (BF16 path)")
     p.add_argument("--train-queries", type=int, default=20000)
+    p.add_argument("--max-pq", type=int, default=1000, help="largest pq of the sweep (--mode learned)")
     p.add_argument("--recall-slack", type=float, default=0.004,
                    help="validation recall@10 the exit may give up against the same search without it")
     args = p.parse_args()
     if args.workload is None:
-        args.workload = "precision-1m-960d-cos" if args.mode == "precision" else "scale-1m-128d-l2"
+        args.workload = {"precision": "precision-1m-960d-cos", "learned": "learned-3m-256d-l2"}.get(
+            args.mode, "scale-1m-128d-l2")
     return args
 
 
@@ -495,7 +498,10 @@ def run_precision(args, torch, local):
     dq = torch.from_numpy(queries).cuda()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     exact = kernel_formula_fp64(w.metric, queries, data[gt_ids])  # nq x k, FP64 of the FP32 rows
-    pqs = [args.pq] if args.pq else [100, 200, 400, 800]
+    # vertex 0 stays far below the target on this workload; the entry-point
+    # rows go to pq 1000
+    pqs_of = {"vertex 0": [args.pq] if args.pq else [100, 400, 1000]}
+    pqs_entries = [args.pq] if args.pq else [100, 200, 400, 800, 1000]
     table, errors = [], {}
     recall_f32 = {}
     for storage in ("f32", "bf16", "fp8"):
@@ -514,8 +520,8 @@ def run_precision(args, torch, local):
         run = Runner(ix, dq, k, stream)
         starts = [("vertex 0", None)]
         if args.entries > 0:
-            # two-level choice for rows of up to 364 floats, else a flat set of at most 4096
-            two = w.dim <= 364 and args.coarse > 0
+            # the two-level choice (any row width up to 4840 floats)
+            two = args.coarse > 0
             n_ent = args.entries if two else min(args.entries, 4096)
             starts.append(("nearest %d of %d entries%s" % (args.starts, n_ent, " (%d clusters, %d probed)"
                                                            % (args.coarse, args.probes) if two else ""),
@@ -526,7 +532,7 @@ def run_precision(args, torch, local):
             for rerank in ((0,) if storage == "f32" else (0, -1)):
                 if storage != "f32":
                     ix.set_rerank(rerank)
-                for pq in pqs:
+                for pq in pqs_of.get(start, pqs_entries):
                     run(pq, stats=True)
                     rec = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
                     for _ in range(2):
@@ -543,16 +549,24 @@ def run_precision(args, torch, local):
                     table.append(row)
                     log("[precision] %s" % row)
         ix.free()
-    # headline: the fastest configuration that loses at most 0.002 recall
-    ok = [r for r in table if r["recall_loss_vs_f32"] <= 0.002]
-    best = max(ok, key=lambda r: r["qps"])
-    line = {"metric": "queries/s within 0.002 recall@%d of FP32 storage, %s" % (k, w.name),
+    # headline: the fastest configuration reaching the recall target; beside
+    # it the fastest such row of each storage (with and without rerank)
+    key = "recall_at_%d" % k
+    ok = [r for r in table if r[key] >= args.recall]
+    per_storage = {}
+    for r in ok:
+        name = r["storage"] + ("" if r["storage"] == "f32" else " rerank " + r["rerank"])
+        if name not in per_storage or r["qps"] > per_storage[name]["qps"]:
+            per_storage[name] = r
+    best = max(ok, key=lambda r: r["qps"]) if ok else max(table, key=lambda r: r[key])
+    line = {"metric": "queries/s at recall@%d>=%.2f, %s" % (k, args.recall, w.name),
             "value": best["qps"], "unit": "queries/s", "n_gpus": 1, "steps": 3, "warmup": 2,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "%s storage, f32 accumulate" % best["storage"],
             "data": "synthetic (seeded Gaussian mixture, GIST1M shape)",
             "config": {"workload": w.name, "n": w.n, "dim": w.dim, "metric": w.metric, "top_k": k,
-                       "queries": nq, "best": best, "table": table,
+                       "queries": nq, "best": best, "best_at_target_per_storage": per_storage,
+                       "reached_target": bool(ok), "table": table,
                        "distance_error_vs_fp64": errors,
                        "distance_error_note": "search distance formula evaluated in FP64 on the stored (decoded) "
                                               "row vs on the FP32 row, over every exact top-k pair",
@@ -684,6 +698,98 @@ def run_build(args, torch, local):
 
 
 # ---------------------------------------------------------------------------
+# learned: the early exit against the search without it and against a fixed
+# hop budget, from vertex 0 and from entry points
+# ---------------------------------------------------------------------------
+
+def convergence_hops(ix, queries, pq, k):
+    """Mean hop after which each query's top-k no longer changes (the labels of
+    the plain search's traces), and the mean hops of that search: the room an
+    exit has."""
+    from song_gb300 import learned as LE
+    X, y = LE.trace_dataset(ix, queries, pq, k, max_samples_per_query=0)
+    nq = queries.shape[0]
+    return float((1.0 - y).sum().item()) / nq, float(X.shape[0]) / nq
+
+
+def run_learned(args, torch, local):
+    """--mode learned: on the workload (default learned-3m-256d-l2), per start
+    (vertex 0, entry points): the plain FP32 search at the smallest pq <=
+    --max-pq reaching the recall target, the exit trained on traces of
+    --train-queries training queries at that pq, a fixed hop budget of the
+    exit's mean hops, and the exit with BF16 rows + FP32 rerank; all on the
+    held-out query set."""
+    import song_gb300 as S
+    from song_gb300 import datasets as D
+    from song_gb300 import learned as LE
+    S.load_library()
+    w, data, queries, graph = load_workload(args)
+    nq, k = queries.shape[0], args.topk
+    _, _, kth10 = ground_truth(args, w, data, queries, k)
+    stream = torch.cuda.current_stream()
+    dq = torch.from_numpy(queries).cuda()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    train_q = D.query_vectors(w, nq=args.train_queries, seed=D.SEED_TRAIN)
+    sweep = [p for p in PQ_SWEEP if p <= args.max_pq] or [args.max_pq]
+    entries = S.sample_entries(w.n, args.entries, seed=D.SEED_BASE + 10, shuffle=True) if args.entries > 0 else None
+    studies = {}
+    for start in ("vertex 0", "entries"):
+        if start == "entries" and entries is None:
+            continue
+        ix = S.Index(graph, data, w.shift, w.metric, device=local)
+        if start == "entries":
+            ix.set_entries(entries, starts=args.starts, coarse=args.coarse, probes=args.probes)
+        run = Runner(ix, dq, k, stream)
+        pq, psweep = (args.pq, []) if args.pq else sweep_pq(torch, run, w, data, queries, kth10, k, args.recall,
+                                                            False, "plain " + start, sweep=sweep)
+        plain = measure_arm(torch, run, pq, 5, flush, stream, data, queries, kth10, w)
+        ix.set_hop_limit(1 << 30)  # the learned kernel without an exit (its exact visited set)
+        noexit = measure_arm(torch, run, pq, 5, flush, stream, data, queries, kth10, w)
+        ix.set_hop_limit(0)
+        conv, traced = convergence_hops(ix, queries, pq, k)
+        model = LE.fit(ix, train_q, pq, k, epochs=6, data=data, metric=w.metric, recall_slack=args.recall_slack,
+                       log=log)
+        ix.set_early_exit(model.params, model.threshold, model.min_hops, model.every)
+        learned = measure_arm(torch, run, pq, 5, flush, stream, data, queries, kth10, w)
+        ix.set_early_exit(None)
+        budget = max(1, int(round(learned["mean_hops"])))
+        ix.set_hop_limit(budget)
+        fixed = measure_arm(torch, run, pq, 5, flush, stream, data, queries, kth10, w)
+        ix.set_hop_limit(0)
+        ixb = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
+        ixb.set_rerank(args.rerank)
+        if start == "entries":
+            ixb.set_entries(entries, starts=args.starts, coarse=args.coarse, probes=args.probes)
+        ixb.set_early_exit(model.params, model.threshold, model.min_hops, model.every)
+        learned_bf16 = measure_arm(torch, Runner(ixb, dq, k, stream), pq, 5, flush, stream, data, queries, kth10, w)
+        ixb.free()
+        ix.free()
+        studies[start] = {
+            "pq": pq, "plain_fp32": plain, "exit_free_learned_kernel": noexit, "learned_fp32": learned,
+            "fixed_budget": dict(fixed, max_hops=budget), "learned_bf16_rerank": learned_bf16,
+            "topk_final_after_hops_mean": round(conv, 2), "traced_hops_mean": round(traced, 2),
+            "speedup_learned_fp32_vs_plain": round(learned["qps"] / plain["qps"], 3),
+            "speedup_learned_bf16_vs_plain": round(learned_bf16["qps"] / plain["qps"], 3),
+            "recall_gain_vs_fixed_budget": round(learned["recall_at_10"] - fixed["recall_at_10"], 4),
+            "model": {"threshold": model.threshold, "min_hops": model.min_hops, "every": model.every,
+                      "train": {kk: model.info[kk] for kk in ("samples", "positive", "trace_s", "train_s", "losses",
+                                                              "chosen", "val_recall_no_exit")}},
+            "plain_pq_sweep_recall_qps": psweep}
+        log("[learned] %s: %s" % (start, studies[start]))
+    ok = [(s, v) for s, v in studies.items() if v["learned_bf16_rerank"]["recall_at_10"] >= args.recall]
+    pick = max(ok or studies.items(), key=lambda sv: sv[1]["learned_bf16_rerank"]["qps"])
+    line = {"metric": "queries/s at recall@10>=%.2f, %s: learned exit + BF16 vs plain FP32" % (args.recall, w.name),
+            "value": pick[1]["learned_bf16_rerank"]["qps"], "unit": "queries/s", "n_gpus": 1, "steps": 5,
+            "warmup": 2, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 storage, f32 accumulate, f32 rerank", "data": "synthetic (seeded Gaussian mixture)",
+            "config": dict(common_config(args, w, nq), train_queries=args.train_queries, max_pq=args.max_pq,
+                           reported_start=pick[0], reached_target=bool(ok), studies=studies,
+                           mlp="5 -> 32 -> 32 -> 1, BF16 weights, FP32 accumulate, trained by the library's kernels",
+                           l2="flushed between steps (256 MB write)")}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # the default mode: plain / entries / learned arms
 # ---------------------------------------------------------------------------
 
@@ -774,7 +880,7 @@ def run_search(args, torch, rank, world, local, dist):
 
     # ---- the same search from each query's nearest entry vertices ----------
     ent, ixe, rune, table, top100 = None, None, None, [], None
-    if args.mode in ("best", "entries", "learned") and entries is not None:
+    if args.mode in ("best", "entries") and entries is not None:
         ixe = S.Index(graph, data, w.shift, w.metric, device=local)
         with_entries(ixe)
         rune = Runner(ixe, dq, k, stream)
@@ -789,7 +895,7 @@ def run_search(args, torch, rank, world, local, dist):
 
     # ---- learned early exit + BF16 storage + FP32 rerank, same starts --------
     lrn, ixl, runl, model = None, None, None, None
-    if args.mode in ("best", "learned"):
+    if args.mode == "best":
         ixl = S.Index(graph, data, w.shift, w.metric, storage="bf16", device=local)
         ixl.set_rerank(args.rerank)
         with_entries(ixl)
@@ -1018,6 +1124,8 @@ def main():
         run_serve(args, torch, local)
     elif args.mode == "build":
         run_build(args, torch, local)
+    elif args.mode == "learned":
+        run_learned(args, torch, local)
     else:
         run_search(args, torch, rank, world, local, dist)
     if dist:

@@ -197,7 +197,7 @@ int song_index_set_entries(song_index *index, const uint64_t *ids, int count, in
  * query then probes its `probes` nearest coarse entries and starts from the
  * `starts` nearest entries of those clusters (starts <= probes <= min(
  * SONG_MAX_STARTS, coarse)): one pass over the coarse rows and the probed
- * clusters instead of all entries.  Distinct ids; rows of up to 364 floats.
+ * clusters instead of all entries.  Distinct ids; rows of up to 4840 floats.
  * Replaces any entries set before; song_index_set_entries(ix, NULL, 0, 1)
  * clears them. */
 #define SONG_MAX_ENTRIES_2LEVEL (1 << 20)

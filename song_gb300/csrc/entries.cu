@@ -382,26 +382,39 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-constexpr int TB_WARPS = 8;                  // warps per block
-constexpr int TB_QUERIES = 4 * TB_WARPS;     // queries per block: 4 per warp
-constexpr int TB_ROWS = 32;                  // rows per staged tile: 4 groups of 8
+// Block shape of the two kernels: `warps` warps (4 queries each), row tiles
+// of `rows` rows (a multiple of 8), nbuf tiles in flight.  Wide rows get
+// smaller blocks and tiles so that a block fits its shared memory.
+struct TileShape {
+  int warps, rows, nbuf;
+  size_t smem(int dpad) const {
+    return sizeof(float) * static_cast<size_t>(dpad) * (4 * warps + static_cast<size_t>(nbuf) * rows);
+  }
+};
 
-// Shared memory of a block: the staged queries, then nbuf row tiles.
-size_t tiled_smem(int dpad, int nbuf) {
-  return sizeof(float) * static_cast<size_t>(dpad) * (TB_QUERIES + static_cast<size_t>(nbuf) * TB_ROWS);
+TileShape tile_shape(int dpad) {
+  TileShape t{8, 32, 2};
+  const size_t budget = 100u * 1024u;
+  while (t.smem(dpad) > budget) {
+    if (t.nbuf == 2) t.nbuf = 1;
+    else if (t.rows > 8) t.rows /= 2;
+    else if (t.warps > 1) t.warps /= 2;
+    else break;
+  }
+  return t;
 }
 
 // Streams rows [r0, r1) of the row-major block `rows` (dpad floats each)
-// through nbuf shared-memory tiles of TB_ROWS rows (the next tile's copies in
+// through nbuf shared-memory tiles of tile_rows rows (the next tile's copies in
 // flight while the current one is scored) and calls score(first_row, n, tile)
 // for each; every thread of the block takes part.  Only rows below r1 are
 // copied.
 template <class F>
-__device__ __forceinline__ void stream_rows(const float *rows, int dpad, int r0, int r1, int nbuf, float *xb,
-                                            F &&score) {
-  const size_t tile = static_cast<size_t>(dpad) * TB_ROWS;
+__device__ __forceinline__ void stream_rows(const float *rows, int dpad, int r0, int r1, int tile_rows, int nbuf,
+                                            float *xb, F &&score) {
+  const size_t tile = static_cast<size_t>(dpad) * tile_rows;
   auto issue = [&](int first, float *buf) {
-    const int n = min(TB_ROWS, r1 - first);
+    const int n = min(tile_rows, r1 - first);
     const float4 *src = reinterpret_cast<const float4 *>(rows + static_cast<size_t>(first) * dpad);
     float4 *dst = reinterpret_cast<float4 *>(buf);
     const int n4 = n * (dpad / 4);
@@ -409,12 +422,12 @@ __device__ __forceinline__ void stream_rows(const float *rows, int dpad, int r0,
     cp_async_commit();
   };
   if (nbuf == 2 && r0 < r1) issue(r0, xb);
-  for (int first = r0, k = 0; first < r1; first += TB_ROWS, ++k) {
+  for (int first = r0, k = 0; first < r1; first += tile_rows, ++k) {
     float *cur = xb + (nbuf == 2 ? static_cast<size_t>(k & 1) * tile : 0);
     if (nbuf == 2) {
       // the other buffer was last read before the previous iteration's closing barrier
-      if (first + TB_ROWS < r1) {
-        issue(first + TB_ROWS, xb + static_cast<size_t>((k + 1) & 1) * tile);
+      if (first + tile_rows < r1) {
+        issue(first + tile_rows, xb + static_cast<size_t>((k + 1) & 1) * tile);
       } else {
         cp_async_commit();
       }
@@ -424,7 +437,7 @@ __device__ __forceinline__ void stream_rows(const float *rows, int dpad, int r0,
       cp_async_wait<0>();
     }
     __syncthreads();  // every thread's copies (and the staged queries) are visible
-    score(first, min(TB_ROWS, r1 - first), cur);
+    score(first, min(tile_rows, r1 - first), cur);
     __syncthreads();
   }
 }
@@ -432,19 +445,20 @@ __device__ __forceinline__ void stream_rows(const float *rows, int dpad, int r0,
 // Two-level choice, first kernel: each query's `probes` nearest coarse
 // entries (positions in the coarse list, which is sorted by id, so the
 // position is the tie order), and the number of probes of each cluster.
-// A block takes 32 queries (4 per warp) and streams all coarse rows; lane l
-// of a warp scores its query l >> 3 against rows l & 7 of each group of 8.
+// A block takes 4 queries per warp and streams all coarse rows; lane l of a
+// warp scores its query l >> 3 against rows l & 7 of each group of 8.
 template <int METRIC, int NP>
-__global__ void __launch_bounds__(TB_WARPS * 32) heads_tiled_kernel(const float *queries, int nq, int dim, int dpad,
-                                                                    const float *coarse_rows, int n_coarse,
-                                                                    int probes, int nbuf, uint32_t *probe_out,
-                                                                    uint32_t *cl_count) {
+__global__ void __launch_bounds__(256) heads_tiled_kernel(const float *queries, int nq, int dim, int dpad,
+                                                          const float *coarse_rows, int n_coarse, int probes,
+                                                          int tile_rows, int nbuf, uint32_t *probe_out,
+                                                          uint32_t *cl_count) {
   extern __shared__ __align__(16) float smt[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int q0 = blockIdx.x * TB_QUERIES;
+  const int bq = 4 * (blockDim.x >> 5);  // queries per block
+  const int q0 = blockIdx.x * bq;
   float *qs = smt;
-  float *xb = smt + static_cast<size_t>(dpad) * TB_QUERIES;
-  for (int i = threadIdx.x; i < TB_QUERIES * dpad; i += blockDim.x) {
+  float *xb = smt + static_cast<size_t>(dpad) * bq;
+  for (int i = threadIdx.x; i < bq * dpad; i += blockDim.x) {
     const int r = i / dpad, j = i - r * dpad;
     qs[i] = (q0 + r < nq && j < dim) ? queries[static_cast<size_t>(q0 + r) * dim + j] : 0.0f;
   }
@@ -456,7 +470,7 @@ __global__ void __launch_bounds__(TB_WARPS * 32) heads_tiled_kernel(const float 
     pi[m] = 0xffffffffu;
   }
   const float *qw = qs + static_cast<size_t>(4 * warp) * dpad;
-  stream_rows(coarse_rows, dpad, 0, n_coarse, nbuf, xb, [&](int first, int n, const float *cur) {
+  stream_rows(coarse_rows, dpad, 0, n_coarse, tile_rows, nbuf, xb, [&](int first, int n, const float *cur) {
     for (int g = 0; g < n; g += 8) {
       const float d = warp_tile_distance<METRIC>(qw, dpad, cur + static_cast<size_t>(g) * dpad, dpad, dpad, lane);
       const int r = g + (lane & 7);
@@ -522,30 +536,29 @@ __global__ void cluster_scatter_kernel(const uint32_t *probe, int total, uint32_
 
 // Two-level choice, second kernel: block c scores cluster c's entries
 // (rows row_offs[c] .. row_offs[c+1] of the cluster-ordered block) against
-// every query that probes it, 32 queries at a time, and writes each
+// every query that probes it, 4 per warp at a time, and writes each
 // (query, probe) pair's NS nearest entries, ascending, to part_*.
 template <int METRIC, int NS>
-__global__ void __launch_bounds__(TB_WARPS * 32) clusters_tiled_kernel(const float *queries, int dim, int dpad,
-                                                                       const float *fine_rows,
-                                                                       const uint32_t *fine_ids,
-                                                                       const uint32_t *row_offs,
-                                                                       const uint32_t *q_offs, const uint32_t *q_list,
-                                                                       int probes, int nbuf, float *part_d,
-                                                                       uint32_t *part_i) {
+__global__ void __launch_bounds__(256) clusters_tiled_kernel(const float *queries, int dim, int dpad,
+                                                             const float *fine_rows, const uint32_t *fine_ids,
+                                                             const uint32_t *row_offs, const uint32_t *q_offs,
+                                                             const uint32_t *q_list, int probes, int tile_rows,
+                                                             int nbuf, float *part_d, uint32_t *part_i) {
   extern __shared__ __align__(16) float smt[];
   const int c = blockIdx.x;
   const uint32_t a0 = q_offs[c], a1 = q_offs[c + 1];
   if (a0 == a1) return;  // no query probes this cluster (uniform over the block)
   const int r0 = static_cast<int>(row_offs[c]), r1 = static_cast<int>(row_offs[c + 1]);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int bq = 4 * (blockDim.x >> 5);  // queries per pass
   float *qs = smt;
-  float *xb = smt + static_cast<size_t>(dpad) * TB_QUERIES;
+  float *xb = smt + static_cast<size_t>(dpad) * bq;
   const float *qw = qs + static_cast<size_t>(4 * warp) * dpad;
-  for (uint32_t qb = a0; qb < a1; qb += TB_QUERIES) {
-    const int nqb = static_cast<int>(min(static_cast<uint32_t>(TB_QUERIES), a1 - qb));
+  for (uint32_t qb = a0; qb < a1; qb += bq) {
+    const int nqb = static_cast<int>(min(static_cast<uint32_t>(bq), a1 - qb));
     const bool busy = 4 * warp < nqb;  // warp-uniform
     __syncthreads();  // the previous query tile is no longer read
-    for (int i = threadIdx.x; i < TB_QUERIES * dpad; i += blockDim.x) {
+    for (int i = threadIdx.x; i < bq * dpad; i += blockDim.x) {
       const int r = i / dpad, j = i - r * dpad;
       float v = 0.0f;
       if (r < nqb && j < dim) v = queries[static_cast<size_t>(q_list[qb + r] / probes) * dim + j];
@@ -558,7 +571,7 @@ __global__ void __launch_bounds__(TB_WARPS * 32) clusters_tiled_kernel(const flo
       bd[m] = __int_as_float(0x7f800000);
       bi[m] = 0xffffffffu;
     }
-    stream_rows(fine_rows, dpad, r0, r1, nbuf, xb, [&](int first, int n, const float *cur) {
+    stream_rows(fine_rows, dpad, r0, r1, tile_rows, nbuf, xb, [&](int first, int n, const float *cur) {
       if (!busy) return;
       for (int g = 0; g < n; g += 8) {
         const float d = warp_tile_distance<METRIC>(qw, dpad, cur + static_cast<size_t>(g) * dpad, dpad, dpad, lane);
@@ -602,8 +615,6 @@ __global__ void merge_starts_kernel(const float *part_d, const uint32_t *part_i,
   }
 }
 
-int tiled_nbuf(int dpad) { return tiled_smem(dpad, 2) <= 96u * 1024u ? 2 : 1; }
-
 // Raises a kernel's dynamic shared-memory limit.
 template <class K>
 cudaError_t allow_smem(K kern, size_t bytes) {
@@ -615,8 +626,9 @@ cudaError_t allow_smem(K kern, size_t bytes) {
 cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t *out, cudaStream_t s) {
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
   const int ns = ix->n_starts, np = ix->n_probes, coarse = ix->n_coarse;
-  const int nbuf = tiled_nbuf(dpad);
-  const size_t smem = tiled_smem(dpad, nbuf);
+  const TileShape ts = tile_shape(dpad);
+  const size_t smem = ts.smem(dpad);
+  const int bq = 4 * ts.warps;
   const int NSel = ns <= 1 ? 1 : (ns <= 2 ? 2 : (ns <= 4 ? 4 : 8));
   const int NPsel = np <= 1 ? 1 : (np <= 2 ? 2 : (np <= 4 ? 4 : 8));
   uint32_t *probes = out + static_cast<size_t>(nq) * ns;
@@ -638,20 +650,21 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
   uint32_t *part_i = q_list + pairs + pairs * NSel;
   cudaError_t e = cudaMemsetAsync(ix->d_cl_count, 0, sizeof(uint32_t) * coarse, s);
   if (e != cudaSuccess) return e;
-  const unsigned grid_q = static_cast<unsigned>((nq + TB_QUERIES - 1) / TB_QUERIES);
+  const unsigned grid_q = static_cast<unsigned>((nq + bq - 1) / bq);
 #define SONG_HEADS(M, NP)                                                                                \
   do {                                                                                                   \
     auto k_ = heads_tiled_kernel<M, NP>;                                                                 \
     if ((e = allow_smem(k_, smem)) != cudaSuccess) return e;                                             \
-    k_<<<grid_q, TB_WARPS * 32, smem, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows, coarse, np, nbuf,   \
-                                           probes, ix->d_cl_count);                                      \
+    k_<<<grid_q, ts.warps * 32, smem, s>>>(queries, nq, dim, dpad, ix->d_coarse_rows, coarse, np, ts.rows, \
+                                           ts.nbuf, probes, ix->d_cl_count);                             \
   } while (0)
 #define SONG_CLUSTERS(M, NS)                                                                             \
   do {                                                                                                   \
     auto k_ = clusters_tiled_kernel<M, NS>;                                                              \
     if ((e = allow_smem(k_, smem)) != cudaSuccess) return e;                                             \
-    k_<<<coarse, TB_WARPS * 32, smem, s>>>(queries, dim, dpad, ix->d_entry_rows, ix->d_entry_ids,         \
-                                           ix->d_offsets, q_offs, q_list, np, nbuf, part_d, part_i);     \
+    k_<<<coarse, ts.warps * 32, smem, s>>>(queries, dim, dpad, ix->d_entry_rows, ix->d_entry_ids,         \
+                                           ix->d_offsets, q_offs, q_list, np, ts.rows, ts.nbuf, part_d,  \
+                                           part_i);                                                      \
     merge_starts_kernel<NS><<<(nq + 255) / 256, 256, 0, s>>>(part_d, part_i, nq, np, ns, out);           \
   } while (0)
 #define SONG_HEADS_BY_NP(M)               \
@@ -800,9 +813,9 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
     return fail(SONG_ERR_ARG, "probes must be 1..min(%d, coarse)", SONG_MAX_STARTS);
   if (starts < 1 || starts > probes) return fail(SONG_ERR_ARG, "starts must be 1..probes");
   const int dim = ix->dx.dim, dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
-  // the head kernel's 32-row tile (rows padded to an odd number of 16-byte
-  // units) and one staged query fit 48 KB of shared memory
-  auto fits = [](int dp) { return 32 * (dp / 4 + 1) * 16 + (dp + 32) * 4 <= 48 * 1024; };
+  // the smallest block shape (one warp, 4 queries, one tile of 8 rows) fits
+  // a block's shared memory
+  auto fits = [](int dp) { return TileShape{1, 8, 1}.smem(dp) <= 227u * 1024u; };
   if (!fits(dpad)) {
     int widest = 4;
     while (fits(widest + 4)) widest += 4;

@@ -111,12 +111,13 @@ def test_two_level_entries_match_oracle(song, oracle, name):
         assert np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
 
 
-@pytest.mark.parametrize("dim,metric", [(200, 0), (200, 1), (200, 2), (130, 0)])
+@pytest.mark.parametrize("dim,metric", [(200, 0), (200, 1), (200, 2), (130, 0), (400, 0), (960, 2)])
 def test_two_level_wide_rows_match_oracle(song, oracle, dim, metric):
-    """Rows wider than 128 floats: the cluster kernel's warp reads several
-    32-float groups per row (one partial group at 130), and at 200 floats two
-    coarse tiles no longer fit the head kernel's shared memory, so it stages
-    one tile at a time.  Clusters of ~75 rows take several 32-row batches."""
+    """Rows wider than 128 floats: each lane sums several 32-float groups per
+    row (one partial group at 130); from 200 floats on the blocks stage one
+    row tile at a time, and at 400 and 960 floats they shrink to fewer warps
+    and 8-row tiles to fit shared memory.  Clusters of ~75 rows take several
+    tiles."""
     from song_gb300 import datasets as D
     shift = 5
     data = D.mixture("unit", 700, dim, 8, seed=dim + metric, center_seed=dim + 50)
