@@ -537,7 +537,7 @@ def run_precision(args, torch, local):
                     rec = GT.recall_tie_aware(run.ids(), data, queries, gt_kth, w.metric, k)
                     for _ in range(2):
                         run(pq)
-                    ms = timed_steps(torch, run, pq, 3, flush, stream)
+                    ms, _ = timed_steps(torch, run, pq, 3, flush, stream)
                     qps = nq / (statistics.median(ms) / 1000.0)
                     if storage == "f32":
                         recall_f32[(start, pq)] = rec
