@@ -501,7 +501,7 @@ def run_precision(args, torch, local):
     # vertex 0 stays far below the target on this workload; the entry-point
     # rows go to pq 1000
     pqs_of = {"vertex 0": [args.pq] if args.pq else [100, 400, 1000]}
-    pqs_entries = [args.pq] if args.pq else [100, 200, 400, 800, 1000]
+    pqs_entries = [args.pq] if args.pq else [50, 75, 100, 200, 400]
     table, errors = [], {}
     recall_f32 = {}
     for storage in ("f32", "bf16", "fp8"):
