@@ -504,19 +504,22 @@ def run_precision(args, torch, local):
     pqs_entries = [args.pq] if args.pq else [50, 75, 100, 200, 400]
     table, errors = [], {}
     recall_f32 = {}
-    for storage in ("f32", "bf16", "fp8"):
+    for storage in ("f32", "bf16", "fp8", "bits"):
         ix = S.Index(graph, data, w.shift, w.metric, storage=storage, device=local)
-        uniq = np.unique(gt_ids)
-        rows = np.concatenate([ix.rows(int(i), 1) for i in uniq])
-        dec = S.dequantize_rows(rows, storage, w.dim)
-        pos = np.searchsorted(uniq, gt_ids)
-        approx = kernel_formula_fp64(w.metric, queries, dec[pos])
-        rel = np.abs(approx - exact) / np.maximum(np.abs(exact), 1e-30)
-        errors[storage] = {"rel_err_median": float("%.3g" % np.median(rel)),
-                           "rel_err_p99": float("%.3g" % np.percentile(rel, 99)),
-                           "rel_err_max": float("%.3g" % rel.max()),
-                           "pairs": int(rel.size)}
-        log("[precision] %s distance error vs FP64 over exact top-%d pairs: %s" % (storage, k, errors[storage]))
+        if storage == "bits":  # 256-bit sign codes: Hamming distance has no FP64 counterpart to compare
+            ix.set_hash_planes(S.hash_planes(w.dim))
+        uniq = np.unique(gt_ids) if storage != "bits" else None
+        if storage != "bits":
+            rows = np.concatenate([ix.rows(int(i), 1) for i in uniq])
+            dec = S.dequantize_rows(rows, storage, w.dim)
+            pos = np.searchsorted(uniq, gt_ids)
+            approx = kernel_formula_fp64(w.metric, queries, dec[pos])
+            rel = np.abs(approx - exact) / np.maximum(np.abs(exact), 1e-30)
+            errors[storage] = {"rel_err_median": float("%.3g" % np.median(rel)),
+                               "rel_err_p99": float("%.3g" % np.percentile(rel, 99)),
+                               "rel_err_max": float("%.3g" % rel.max()),
+                               "pairs": int(rel.size)}
+            log("[precision] %s distance error vs FP64 over exact top-%d pairs: %s" % (storage, k, errors[storage]))
         run = Runner(ix, dq, k, stream)
         starts = [("vertex 0", None)]
         if args.entries > 0:

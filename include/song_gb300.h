@@ -58,6 +58,13 @@ extern "C" {
 #define SONG_STORAGE_F32 0
 #define SONG_STORAGE_BF16 1
 #define SONG_STORAGE_FP8 2
+/* 256-bit sign codes searched by Hamming distance: the reference's bit-hash
+ * path (hash_warp_no_heap_astar_accelerator.h:22-41 codes, __popc distances
+ * :96-104, 226-235) as a row format of the same search; needs the index's
+ * hyperplanes (song_index_set_hash_planes) before the first search, and
+ * re-ranks the final candidates with FP32 distances of the index's metric. */
+#define SONG_STORAGE_BITS 3
+#define SONG_HASH_BITS 256
 
 /* Limits of this implementation. */
 #define SONG_MAX_PQ 1023   /* the reference's FixHash casts its slot to short: 8*pq < 32768 */
@@ -158,6 +165,15 @@ int song_index_rows(const song_index *index, uint64_t first, uint64_t count, voi
 #define SONG_MLP_PARAMS 1281
 int song_index_set_early_exit(song_index *index, const float *weights, float threshold,
                               int min_hops, int every);
+
+/* Hyperplanes of a SONG_STORAGE_BITS index (hash_warp_no_heap_astar_accelerator.h:
+ * 22-41; bithash.h:8-65): planes holds SONG_HASH_BITS rows of dim floats.
+ * Bit i of a vector's code is set when its dot product with plane i is >= 0,
+ * the dot product summed as the search sums distances (lane l of a warp takes
+ * dimensions l, l+32, ... with fused multiply-adds; the 32 partial sums meet
+ * in the xor butterfly).  Computes the codes of all base vectors; queries are
+ * coded the same way on every search. */
+int song_index_set_hash_planes(song_index *index, const float *planes);
 
 /* Fixed hop budget (0 = off): stop every query after max_hops expansions.
  * A baseline heuristic to compare the learned exit against; no counterpart

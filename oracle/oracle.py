@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libsong_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
-L2, IP, COS = 0, 1, 2
+L2, IP, COS, HAMMING = 0, 1, 2, 3
 METRICS = {"l2": L2, "ip": IP, "cos": COS}
 MODE_REF, MODE_LEX, MODE_LEX_EXACT = 0, 1, 2
 TRACE_FIELDS = 6  # 5 early-exit features + number of changes of the top-k set
@@ -89,6 +89,8 @@ def lib():
         L.orc_nearest_entry.argtypes = [P, P, i32, P, i32, i32, i32, P]
         L.orc_kernel_search_trace.restype = i32
         L.orc_kernel_search_trace.argtypes = [P, P, i32, i32, i32, i32, i32, P, P, P, P, P, P]
+        L.orc_hash_codes.restype = i32
+        L.orc_hash_codes.argtypes = [P, ctypes.c_uint64, i32, P, i32, P]
         L.orc_graph_build.restype = i32
         L.orc_graph_build.argtypes = [P, ctypes.c_uint64, i32, i32, i32, i32, i32, i32, i32, i32, P]
         L.orc_cpu_search.restype = i32
@@ -219,6 +221,19 @@ class OracleIndex:
         if rc != 0:
             raise ValueError("orc_cpu_search failed")
         return out, ex
+
+
+def hash_codes(rows, planes, use_fma=True):
+    """256-bit sign codes (n x 8 uint32) of rows from 256 hyperplanes, summed as
+    the kernel sums (orc_hash_codes)."""
+    rows = np.ascontiguousarray(rows, dtype=np.float32)
+    planes = np.ascontiguousarray(planes, dtype=np.float32)
+    n, dim = rows.shape
+    assert planes.shape == (256, dim)
+    out = np.empty((n, 8), dtype=np.uint32)
+    if lib().orc_hash_codes(_ptr(rows), n, dim, _ptr(planes), int(use_fma), _ptr(out)) != 0:
+        raise ValueError("orc_hash_codes failed")
+    return out
 
 
 def graph_build(data, metric, shift=5, search_degree=15, fixed_degree=31, budget=150, batch_div=0, nthreads=None):

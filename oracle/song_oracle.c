@@ -23,6 +23,18 @@
  * lanes hold the same value.  Cosine: sign * tmp * tmp / |x|^2 in float with
  * sign = (tmp < 0 ? 1 : -1), 0 when |x|^2 == 0; the query norm is not used. */
 float orc_kernel_distance(int metric, int dim, const float *q, const float *x, int use_fma) {
+  if (metric == ORC_HAMMING) {
+    /* hash_warp_no_heap_astar_accelerator.h:96-104: __popc of the xor of the
+     * code words, summed (an integer, exact as float); dim = code words */
+    uint32_t qa, xa;
+    int h = 0;
+    for (int j = 0; j < dim; ++j) {
+      memcpy(&qa, q + j, 4);
+      memcpy(&xa, x + j, 4);
+      h += __builtin_popcount(qa ^ xa);
+    }
+    return (float)h;
+  }
   float t[32], l[32], nt[32], nl[32];
   for (int lane = 0; lane < 32; ++lane) {
     float a = 0.0f, b = 0.0f;
@@ -690,7 +702,7 @@ static void *kworker(void *arg) {
 static int check_index(const orc_index *ix) {
   if (!ix || !ix->data || !ix->graph || ix->n == 0 || ix->dim <= 0) return -1;
   if (ix->shift < 1 || ix->shift > 12) return -1;
-  if (ix->metric < ORC_L2 || ix->metric > ORC_COS) return -1;
+  if (ix->metric < ORC_L2 || ix->metric > ORC_HAMMING) return -1;
   return 0;
 }
 
@@ -1327,4 +1339,24 @@ int orc_graph_build(const float *data, uint64_t n, int dim, int metric, int shif
   free(b.edge_dist);
   free(res);
   return rc;
+}
+
+/* ------------------------------------------------------------------------- */
+/* 256-bit sign codes (hash_warp_no_heap_astar_accelerator.h:22-41)          */
+/* ------------------------------------------------------------------------- */
+
+/* codes[r*8 + i/32] bit i%32 = (x_r . plane_i >= 0), the dot product summed
+ * as the kernel sums distances (orc_kernel_distance, inner product: partial
+ * sums of lane-strided fused multiply-adds, xor butterfly). */
+int orc_hash_codes(const float *rows, uint64_t n, int dim, const float *planes, int use_fma, uint32_t *codes) {
+  if (!rows || !planes || !codes || dim <= 0) return -1;
+  for (uint64_t r = 0; r < n; ++r) {
+    const float *x = rows + r * (uint64_t)dim;
+    for (int w = 0; w < 8; ++w) codes[r * 8 + w] = 0u;
+    for (int i = 0; i < 256; ++i) {
+      const float t = -orc_kernel_distance(ORC_IP, dim, x, planes + (size_t)i * (size_t)dim, use_fma);
+      if (t >= 0.0f) codes[r * 8 + (i >> 5)] |= 1u << (i & 31);
+    }
+  }
+  return 0;
 }

@@ -42,7 +42,8 @@
 extern "C" {
 #endif
 
-enum { ORC_L2 = 0, ORC_IP = 1, ORC_COS = 2 };      /* KernelFixedDegreeGraph<0|1|2> */
+enum { ORC_L2 = 0, ORC_IP = 1, ORC_COS = 2,       /* KernelFixedDegreeGraph<0|1|2> */
+       ORC_HAMMING = 3 };                         /* rows are 256-bit codes (8 words, dim = 8) */
 /* ORC_MODE_LEX_EXACT: LEX with an exact visited multiset instead of FixHash
  * (the learned/low-precision kernel's visited set, which never loses an entry). */
 enum { ORC_MODE_REF = 0, ORC_MODE_LEX = 1, ORC_MODE_LEX_EXACT = 2 };
@@ -140,6 +141,10 @@ int orc_classify(const orc_event *a, int na, const orc_event *b, int nb, int *at
 
 /* CPU best-first search of graph.h:169-216 with result size k.  out: nq x k
  * (ORC_NO_ID past the result length); explored may be NULL. */
+/* 256-bit sign codes of n rows from 256 hyperplanes (planes: 256 x dim),
+ * codes: n x 8 words, bit i = (row . plane_i >= 0) summed as the kernel sums. */
+int orc_hash_codes(const float *rows, uint64_t n, int dim, const float *planes, int use_fma, uint32_t *codes);
+
 /* The reference's CPU graph builder (graph.h:149-167 with graph.h:32-55,
  * 98-137): batch_div 0 inserts one vertex at a time (the reference's graph);
  * batch_div > 0 inserts batches of max(1, inserted / batch_div) vertices,

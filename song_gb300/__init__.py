@@ -33,7 +33,8 @@ SONG_MAX_STARTS = 8
 SONG_MAX_ENTRIES_2LEVEL = 1 << 20
 SONG_MAX_COARSE = 16384
 METRICS = {"l2": 0, "ip": 1, "cos": 2}
-STORAGES = {"f32": 0, "bf16": 1, "fp8": 2}
+STORAGES = {"f32": 0, "bf16": 1, "fp8": 2, "bits": 3}
+HASH_BITS = 256
 MAX_PQ = 1023
 NO_ID = np.uint64(0xFFFFFFFFFFFFFFFF)
 
@@ -45,6 +46,7 @@ EXPORTED = [
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
     "song_index_set_hop_limit", "song_index_set_timing", "song_index_timing", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
+    "song_index_set_hash_planes",
     "song_server_set_idle_polls", "song_server_running", "song_server_wait", "song_debug_fail_alloc",
     "song_debug_set_wait", "song_debug_server_hold",
 ]
@@ -133,6 +135,8 @@ def load_library():
     L.song_server_result.argtypes = [P, ctypes.c_uint64, P, ctypes.POINTER(i32), ctypes.POINTER(i32)]
     L.song_server_destroy.restype = i32
     L.song_server_destroy.argtypes = [P]
+    L.song_index_set_hash_planes.restype = i32
+    L.song_index_set_hash_planes.argtypes = [P, P]
     L.song_server_set_idle_polls.restype = i32
     L.song_server_set_idle_polls.argtypes = [P, ctypes.c_uint32]
     L.song_server_running.restype = i32
@@ -302,6 +306,14 @@ class Index:
                                                  ctypes.c_void_p(evals_ptr) if evals_ptr else None,
                                                  ctypes.c_void_p(stream) if stream else None))
 
+    def set_hash_planes(self, planes):
+        """SONG_STORAGE_BITS: the HASH_BITS x dim hyperplanes of the 256-bit
+        sign codes; codes every base vector (song_index_set_hash_planes)."""
+        h = np.ascontiguousarray(planes, dtype=np.float32)
+        if h.shape != (HASH_BITS, self.dim):
+            raise ValueError("planes must be %d x %d" % (HASH_BITS, self.dim))
+        _check(load_library().song_index_set_hash_planes(self._h, _ptr(h)))
+
     def debug_set_wait(self, wait_limit=1 << 24, extra_tx=0):
         """Test hook (song_debug_set_wait): the kernel's bounded waits give up
         after wait_limit polls; extra_tx bytes that no copy delivers make a
@@ -370,6 +382,11 @@ def graph_build_gpu(data, metric, shift=5, search_degree=15, fixed_degree=31, bu
                                                fixed_degree, budget, batch_div, device,
                                                nthreads or os.cpu_count() or 1, _ptr(out)))
     return out
+
+
+def hash_planes(dim, seed=123):
+    """HASH_BITS x dim standard-normal hyperplanes (seeded), for SONG_STORAGE_BITS."""
+    return np.random.default_rng(seed).standard_normal((HASH_BITS, dim)).astype(np.float32)
 
 
 def debug_fail_alloc(n):

@@ -106,6 +106,8 @@ void release(song_index *ix) {
   cudaFree(ix->d_cl_count);
   cudaFree(ix->d_entry_work);
   cudaFree(ix->d_starts);
+  cudaFree(ix->d_planes);
+  cudaFree(ix->d_qcodes);
   for (cudaEvent_t &e : ix->ev)
     if (e) cudaEventDestroy(e);
   if (ix->stream) cudaStreamDestroy(ix->stream);
@@ -125,6 +127,16 @@ int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_
   c.counter = ix->d_counter;
   c.error = ix->d_error;
   song::apply_index_settings(ix, c);
+  if (ix->dx.storage == SONG_STORAGE_BITS) {
+    // the queries' 256-bit codes, on the search's stream
+    if (!ix->has_planes) return fail(SONG_ERR_ARG, "SONG_STORAGE_BITS index without hash planes");
+    int rc = grow(&ix->d_qcodes, &ix->cap_qcodes, static_cast<size_t>(nq) * 8, &ix->device_bytes);
+    if (rc) return rc;
+    const int e = song::launch_hash_codes(d_q, static_cast<uint64_t>(nq), ix->dx.dim, ix->dx.dim, ix->d_planes,
+                                          static_cast<int>(ix->dx.f32_row_bytes / 4), ix->d_qcodes, s);
+    if (e != 0) return fail(SONG_ERR_CUDA, "query codes: %s", cudaGetErrorString((cudaError_t)e));
+    c.qcodes = ix->d_qcodes;
+  }
   if (ix->timing) SONG_CUDA(cudaEventRecord(ix->ev[0], s));
   int rc = song::prepare_starts(ix, c, s);
   if (rc != SONG_OK) return rc;
@@ -221,7 +233,7 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   if (shift < 1 || shift > SONG_MAX_SHIFT)
     return fail(SONG_ERR_ARG, "shift must be in [1, %d]", SONG_MAX_SHIFT);
   if (metric < SONG_METRIC_L2 || metric > SONG_METRIC_COS) return fail(SONG_ERR_ARG, "bad metric");
-  if (storage < SONG_STORAGE_F32 || storage > SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "bad storage %d", storage);
+  if (storage < SONG_STORAGE_F32 || storage > SONG_STORAGE_BITS) return fail(SONG_ERR_ARG, "bad storage %d", storage);
 
   // The reference reads degree and ids unchecked (warp_astar_accelerator.h:212-214);
   // a malformed row would make it read out of bounds, so reject it here.
@@ -262,6 +274,9 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
   } else if (storage == SONG_STORAGE_BF16) {
     dx.dpad = (dim + 7) / 8 * 8;
     dx.row_bytes = static_cast<uint32_t>(dx.dpad) * 2u;
+  } else if (storage == SONG_STORAGE_BITS) {
+    dx.dpad = SONG_HASH_BITS / 32;  // code words
+    dx.row_bytes = SONG_HASH_BITS / 8;
   } else {
     dx.dpad = (dim + 15) / 16 * 16;
     dx.scale_off = static_cast<uint32_t>(dx.dpad);
@@ -294,7 +309,9 @@ int song_index_create(const uint64_t *graph, const float *data, uint64_t n, int 
     SONG_CUDA_IX(song::dev_malloc(&ix->d_rows, rows_bytes));
     ix->device_bytes += rows_bytes;
     const uint32_t in_floats = dx.f32_row_bytes / 4u;
-    if (storage == SONG_STORAGE_BF16)
+    if (storage == SONG_STORAGE_BITS)  // codes follow from the planes (song_index_set_hash_planes)
+      SONG_CUDA_IX(cudaMemsetAsync(ix->d_rows, 0, rows_bytes, ix->stream));
+    else if (storage == SONG_STORAGE_BF16)
       to_bf16_kernel<<<4 * 152, 256, 0, ix->stream>>>(ix->d_rows_f32, in_floats, n, dim, dx.dpad,
                                                       static_cast<__nv_bfloat16 *>(ix->d_rows));
     else
@@ -483,7 +500,7 @@ int song_index_set_early_exit(song_index *ix, const float *weights, float thresh
     return SONG_OK;
   }
   if (every < 1 || min_hops < 0) return fail(SONG_ERR_ARG, "every must be >= 1 and min_hops >= 0");
-  if (ix->dx.storage == SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "early exit is built for F32 and BF16 storage");
+  if (ix->dx.storage >= SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "early exit is built for F32 and BF16 storage");
   std::vector<__nv_bfloat16> w(SONG_MLP_PARAMS);
   for (int i = 0; i < SONG_MLP_PARAMS; ++i) w[i] = __float2bfloat16_rn(weights[i]);
   if (!ix->d_mlp) {
@@ -528,7 +545,7 @@ int song_index_set_hop_limit(song_index *ix, int max_hops) {
   g_last_error.clear();
   if (!ix) return fail(SONG_ERR_ARG, "null index");
   if (max_hops < 0) return fail(SONG_ERR_ARG, "max_hops must be >= 0");
-  if (max_hops > 0 && ix->dx.storage == SONG_STORAGE_FP8)
+  if (max_hops > 0 && ix->dx.storage >= SONG_STORAGE_FP8)
     return fail(SONG_ERR_ARG, "the hop limit is built for F32 and BF16 storage");
   ix->max_hops = max_hops;
   return SONG_OK;
@@ -543,7 +560,7 @@ int song_search_trace_device(song_index *ix, const float *d_queries, int nq, int
   if (nq == 0) return SONG_OK;
   if (!d_queries || !d_out || !d_trace || !d_final || trace_hops < 1)
     return fail(SONG_ERR_ARG, "null buffer or trace_hops < 1");
-  if (ix->dx.storage == SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "tracing is built for F32 and BF16 storage");
+  if (ix->dx.storage >= SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "tracing is built for F32 and BF16 storage");
   DeviceGuard g(ix->device);
   if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);

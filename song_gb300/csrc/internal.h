@@ -44,6 +44,7 @@ struct SearchCall {
   int32_t *trace_final = nullptr;  // nq x 2: final top-k version, hops traced
   const uint32_t *starts = nullptr;  // nq x n_starts start vertices (entry points), null = vertex 0
   int n_starts = 1;
+  const uint32_t *qcodes = nullptr;  // BITS storage: nq x 8 query code words
   uint32_t wait_limit = 1u << 24;  // polls of a bounded mbarrier wait
   uint32_t extra_tx = 0;           // test hook (song_debug_set_wait)
 };
@@ -56,6 +57,10 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
 uint32_t search_warp_bytes(const DeviceIndex &ix, int pq);
 
 int launch_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *out, cudaStream_t s);
+
+// BITS storage: the 256-bit codes of n vectors (search_bits.cu).
+int launch_hash_codes(const float *rows, uint64_t n, int stride, int dim, const float *planes, int pstride,
+                      uint32_t *codes, cudaStream_t s);
 
 }  // namespace song
 
@@ -139,6 +144,11 @@ struct song_index {
   bool timing = false;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   bool timed_entries = false;
+  // BITS storage: hyperplanes (SONG_HASH_BITS x f32 row width) and per-call query codes
+  float *d_planes = nullptr;
+  bool has_planes = false;
+  uint32_t *d_qcodes = nullptr;
+  size_t cap_qcodes = 0;
   uint32_t *d_starts = nullptr;
   size_t cap_starts = 0;
   uint64_t device_bytes = 0;

@@ -165,16 +165,18 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
   p.trace_final = c.trace_final;
   p.starts = c.starts;
   p.n_starts = c.starts ? c.n_starts : 1;
+  p.qcodes = c.qcodes;
   p.wait_limit = c.wait_limit;
   p.extra_tx = c.extra_tx;
   if (learned) {
-    if (ix.storage == 2) return -1;
+    if (ix.storage >= 2) return -1;
     return launch_learned(p, ix.storage, ix.metric, L.H, L.S, stream);
   }
   switch (ix.storage) {
     case 0: return launch_f32(p, ix.metric, L.H, L.S, stream);
     case 1: return launch_bf16(p, ix.metric, L.H, L.S, stream);
     case 2: return launch_fp8(p, ix.metric, L.H, L.S, stream);
+    case 3: return c.qcodes ? launch_bits(p, ix.metric, L.S, stream) : -1;  // query codes come from the caller's path
     default: return -1;
   }
 }

@@ -85,6 +85,7 @@ struct Params {
   float *trace;           // [nq][trace_hops][TRACE_FIELDS] or null
   int trace_hops;
   int32_t *trace_final;   // [nq]: final top-k version, hops traced
+  const uint32_t *qcodes; // BITS storage: [nq][8] 256-bit codes of the queries
   const uint32_t *starts; // [nq][n_starts] start vertices of each query, or null: vertex 0
   int n_starts;
   // entry points chosen inside the server's persistent warps (entry_rows
@@ -122,6 +123,11 @@ __device__ __forceinline__ float load_elem(const uint8_t *row, int j, float scal
   return __fmul_rn(__half2float(__half(h)), scale);
 }
 
+// The 256-bit code of a query (BITS storage), in every lane.
+struct Code8 {
+  uint32_t w[8];
+};
+
 // Distances of candidates 0..m-1 (candidate c's id in lane c); candidate c's
 // distance is returned in lane c.  False if a bulk copy never completed.
 // Rows are taken in pairs through the paired FP32 instructions (the same
@@ -130,7 +136,22 @@ __device__ __forceinline__ float load_elem(const uint8_t *row, int j, float scal
 template <int METRIC, int STORAGE, int H>
 __device__ __forceinline__ bool gather_distances(const Params &p, uint8_t *stage, uint64_t *mbar,
                                                  uint32_t &ph0, uint32_t &ph1, const float *qv,
-                                                 int m, uint32_t cid, float &out, int lane) {
+                                                 int m, uint32_t cid, float &out, int lane,
+                                                 const Code8 &qc) {
+  if constexpr (STORAGE == 3) {
+    // Hamming distance of 256-bit codes: lane c reads candidate c's 32-byte
+    // code straight from global memory (two 16-byte loads) and sums the
+    // popcounts of its xor with the query's code (an integer, exact as float)
+    out = 0.0f;
+    if (lane < m) {
+      const uint4 *r = reinterpret_cast<const uint4 *>(p.rows + static_cast<uint64_t>(cid) * 32u);
+      const uint4 a = __ldg(r), b = __ldg(r + 1);
+      const int h = __popc(a.x ^ qc.w[0]) + __popc(a.y ^ qc.w[1]) + __popc(a.z ^ qc.w[2]) + __popc(a.w ^ qc.w[3]) +
+                    __popc(b.x ^ qc.w[4]) + __popc(b.y ^ qc.w[5]) + __popc(b.z ^ qc.w[6]) + __popc(b.w ^ qc.w[7]);
+      out = static_cast<float>(h);
+    }
+    return true;
+  }
   const int nchunks = (m + H - 1) / H;
   const uint32_t rb = p.row_bytes;
   auto issue = [&](int c) {
@@ -345,7 +366,10 @@ struct QueryStats {
 template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
 __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const float *qsrc, const uint32_t *starts,
                                           int ns, int pq, int k, uint64_t *o, float *trace, QueryStats &st,
-                                          int lane) {
+                                          int lane, const uint32_t *qcode = nullptr) {
+  Code8 qc;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) qc.w[i] = STORAGE == 3 ? qcode[i] : 0u;
   typename VisitedOf<LEARNED>::type vh = VisitedOf<LEARNED>::make(w.tab, pq);
   RegQueue<S> Q, T;  // candidate queue and top-pq list, ascending (distance, id)
   constexpr int C = RegQueue<S>::C;
@@ -361,7 +385,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
 
   // warp_astar_accelerator.h:115-176: distances to the starts, queue = {starts}.
   float cd;
-  if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, ns, sid, cd, lane)) {
+  if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, ns, sid, cd, lane, qc)) {
     return false;
   }
   const float d0 = __shfl_sync(FULL, cd, 0);
@@ -436,7 +460,7 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
     __syncwarp();
     const uint32_t cid = lane < m ? w.cbuf[lane] : 0u;
     // :237-287 distances.
-    if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, m, cid, cd, lane))
+    if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, m, cid, cd, lane, qc))
       return false;
     evals += m;
     // The next vertex popped is the smaller of the queue head and the best
@@ -556,8 +580,10 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
   return true;
 }
 
+// Small queues (S <= 4, pq < 128) ask for six resident blocks (24 warps per
+// SM): at most 80 registers, and the per-warp shared memory of such pq fits.
 template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
-__global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(const Params p) {
+__global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, S <= 4 ? 6 : 1) search_kernel(const Params p) {
   extern __shared__ __align__(128) uint8_t smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -598,7 +624,8 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, 1) search_kernel(con
                                                             : nullptr,
                                                    p.n_starts, p.pq,
                                                    p.k, p.out + static_cast<size_t>(qid) * p.k, trace, st,
-                                                   lane)) {
+                                                   lane, STORAGE == 3 ? p.qcodes + static_cast<size_t>(qid) * 8
+                                                                      : nullptr)) {
       if (lane == 0) atomicOr(p.error, 1);
       return;
     }
@@ -673,6 +700,7 @@ int launch_storage(const Params &p, int metric, int H, int S, cudaStream_t s) {
 int launch_f32(const Params &p, int metric, int H, int S, cudaStream_t s);
 int launch_bf16(const Params &p, int metric, int H, int S, cudaStream_t s);
 int launch_fp8(const Params &p, int metric, int H, int S, cudaStream_t s);
+int launch_bits(const Params &p, int metric, int S, cudaStream_t s);
 int launch_learned(const Params &p, int storage, int metric, int H, int S, cudaStream_t s);
 
 }  // namespace song
