@@ -492,13 +492,9 @@ __global__ void __launch_bounds__(256) heads_tiled_kernel(const float *queries, 
 
 // Exclusive scan of the per-cluster probe counts (one block): offs[0..n],
 // and a copy of offs[0..n-1] as the scatter cursors.
-__global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *count, int n, uint32_t *offs,
-                                                            uint32_t *cursor) {
-  __shared__ uint32_t warp_sum[32];
-  const int per = (n + blockDim.x - 1) / blockDim.x;
-  const int b = threadIdx.x * per, e = min(n, b + per);
-  uint32_t s = 0;
-  for (int i = b; i < e; ++i) s += count[i];
+// Exclusive block scan of one value per thread (1024 threads); returns this
+// thread's exclusive prefix, and the total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t s, uint32_t *warp_sum, uint32_t *total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = s;  // inclusive scan within the warp
 #pragma unroll
@@ -506,6 +502,7 @@ __global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *coun
     const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
+  __syncthreads();  // warp_sum may still be read by a previous scan
   if (lane == 31) warp_sum[warp] = x;
   __syncthreads();
   if (warp == 0) {
@@ -518,13 +515,37 @@ __global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *coun
     warp_sum[lane] = w;
   }
   __syncthreads();
-  uint32_t run = x - s + (warp > 0 ? warp_sum[warp - 1] : 0u);
+  *total = warp_sum[(blockDim.x >> 5) - 1];
+  return x - s + (warp > 0 ? warp_sum[warp - 1] : 0u);
+}
+
+// Exclusive scans of the per-cluster probe counts (one block): offs[0..n],
+// a copy of offs[0..n-1] as the scatter cursors, and task_offs[0..n] of the
+// clusters' warp tasks (one per 4 of its queries).
+__global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *count, int n, uint32_t *offs,
+                                                            uint32_t *cursor, uint32_t *task_offs) {
+  __shared__ uint32_t warp_sum[32];
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t s = 0, st = 0;
+  for (int i = b; i < e; ++i) {
+    s += count[i];
+    st += (count[i] + 3u) / 4u;
+  }
+  uint32_t total, ttotal;
+  uint32_t run = block_exclusive_scan(s, warp_sum, &total);
+  uint32_t trun = block_exclusive_scan(st, warp_sum, &ttotal);
   for (int i = b; i < e; ++i) {
     offs[i] = run;
     cursor[i] = run;
     run += count[i];
+    if (task_offs) task_offs[i] = trun;
+    trun += (count[i] + 3u) / 4u;
   }
-  if (threadIdx.x == blockDim.x - 1) offs[n] = run;
+  if (threadIdx.x == 0) {
+    offs[n] = total;
+    if (task_offs) task_offs[n] = ttotal;
+  }
 }
 
 // Inverts the probe lists: list[cursor[c]++] = q * probes + r for every
@@ -595,6 +616,94 @@ __global__ void __launch_bounds__(256) clusters_tiled_kernel(const float *querie
   }
 }
 
+// Two-level choice, second kernel for rows of up to WARP_TASK_DPAD floats:
+// warp tasks of (cluster, 4 of the queries that probe it), taken by
+// persistent warps (task_offs: the scan's per-cluster task offsets).  A warp
+// stages its 4 queries and streams the cluster's rows 8 at a time through a
+// double buffer of its own (cp.async; warp barriers only), scores them as a
+// warp tile, and writes each (query, probe) pair's NS nearest entries.
+constexpr int WARP_TASK_DPAD = 256;
+constexpr int WT_WARPS = 4;  // warps per block
+
+size_t warp_task_smem(int dpad) { return sizeof(float) * static_cast<size_t>(dpad) * (4 + 2 * 8) * WT_WARPS; }
+
+template <int METRIC, int NS>
+__global__ void __launch_bounds__(WT_WARPS * 32) clusters_warp_kernel(const float *queries, int dim, int dpad,
+                                                                      const float *fine_rows,
+                                                                      const uint32_t *fine_ids,
+                                                                      const uint32_t *row_offs,
+                                                                      const uint32_t *q_offs, const uint32_t *q_list,
+                                                                      const uint32_t *task_offs, int n_clusters,
+                                                                      int probes, float *part_d, uint32_t *part_i) {
+  extern __shared__ __align__(16) float smt[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float *qs = smt + static_cast<size_t>(wib) * dpad * (4 + 16);
+  float *xb = qs + static_cast<size_t>(4) * dpad;  // two buffers of 8 rows
+  const uint32_t total = task_offs[n_clusters];
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  const int d4 = dpad / 4;
+  for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + wib; t < total; t += nwarps) {
+    // the cluster of task t: the last c with task_offs[c] <= t
+    int lo = 0, hi = n_clusters - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (task_offs[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const int c = lo;
+    const uint32_t qb = q_offs[c] + 4u * (t - task_offs[c]);
+    const int nqg = static_cast<int>(min(4u, q_offs[c + 1] - qb));
+    const int r0 = static_cast<int>(row_offs[c]), r1 = static_cast<int>(row_offs[c + 1]);
+    __syncwarp();  // the previous task's buffers are no longer read
+    for (int i = lane; i < 4 * dpad; i += 32) {
+      const int a = i / dpad, j = i - a * dpad;
+      qs[i] = (a < nqg && j < dim) ? queries[static_cast<size_t>(q_list[qb + a] / probes) * dim + j] : 0.0f;
+    }
+    float bd[NS];
+    uint32_t bi[NS];
+#pragma unroll
+    for (int m = 0; m < NS; ++m) {
+      bd[m] = __int_as_float(0x7f800000);
+      bi[m] = 0xffffffffu;
+    }
+    auto issue = [&](int first, float *buf) {
+      const int n4 = min(8, r1 - first) * d4;
+      const float4 *src = reinterpret_cast<const float4 *>(fine_rows + static_cast<size_t>(first) * dpad);
+      float4 *dst = reinterpret_cast<float4 *>(buf);
+      for (int i = lane; i < n4; i += 32) cp_async16(dst + i, src + i);
+      cp_async_commit();
+    };
+    issue(r0, xb);
+    for (int first = r0, k = 0; first < r1; first += 8, ++k) {
+      float *cur = xb + static_cast<size_t>(k & 1) * 8 * dpad;
+      if (first + 8 < r1) {
+        issue(first + 8, xb + static_cast<size_t>((k + 1) & 1) * 8 * dpad);
+      } else {
+        cp_async_commit();
+      }
+      cp_async_wait<1>();
+      __syncwarp();  // every lane's copies (and the staged queries) are visible
+      const float d = warp_tile_distance<METRIC>(qs, dpad, cur, dpad, dpad, lane);
+      const int r = first + (lane & 7);
+      if (r < r1) list_insert<NS>(bd, bi, d, fine_ids[r]);
+      __syncwarp();  // this buffer is refilled two rounds on
+    }
+    const int a = lane >> 3;
+    const uint32_t pair = a < nqg ? q_list[qb + a] : 0u;
+    int h = 0;
+#pragma unroll
+    for (int r = 0; r < NS; ++r) {
+      float wd;
+      uint32_t wid;
+      group8_take<NS>(bd, bi, h, wd, wid);
+      if ((lane & 7) == 0 && a < nqg) {
+        part_d[static_cast<size_t>(pair) * NS + r] = wd;
+        part_i[static_cast<size_t>(pair) * NS + r] = wid;
+      }
+    }
+  }
+}
+
 // Each query's ns nearest over its probes' lists, ascending by (distance, id).
 template <int NS>
 __global__ void merge_starts_kernel(const float *part_d, const uint32_t *part_i, int nq, int probes, int ns,
@@ -634,7 +743,7 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
   uint32_t *probes = out + static_cast<size_t>(nq) * ns;
   // work area: cursors, offsets, inverted lists, per-(query, probe) lists
   const size_t pairs = static_cast<size_t>(nq) * np;
-  const size_t need = static_cast<size_t>(coarse) * 2 + 1 + pairs + 2 * pairs * NSel;
+  const size_t need = static_cast<size_t>(coarse) * 3 + 2 + pairs + 2 * pairs * NSel;
   if (need > ix->cap_entry_work) {
     cudaFree(ix->d_entry_work);
     ix->d_entry_work = nullptr;
@@ -648,6 +757,7 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
   uint32_t *q_list = q_offs + coarse + 1;
   float *part_d = reinterpret_cast<float *>(q_list + pairs);
   uint32_t *part_i = q_list + pairs + pairs * NSel;
+  uint32_t *task_offs = part_i + pairs * NSel;  // coarse + 1
   cudaError_t e = cudaMemsetAsync(ix->d_cl_count, 0, sizeof(uint32_t) * coarse, s);
   if (e != cudaSuccess) return e;
   const unsigned grid_q = static_cast<unsigned>((nq + bq - 1) / bq);
@@ -660,6 +770,21 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
   } while (0)
 #define SONG_CLUSTERS(M, NS)                                                                             \
   do {                                                                                                   \
+    if (dpad <= WARP_TASK_DPAD) {                                                                        \
+      auto w_ = clusters_warp_kernel<M, NS>;                                                             \
+      const size_t wsm = warp_task_smem(dpad);                                                           \
+      if ((e = allow_smem(w_, wsm)) != cudaSuccess) return e;                                            \
+      int per_sm = 0, sms = 0, dev = 0;                                                                  \
+      cudaGetDevice(&dev);                                                                               \
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                                 \
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, w_, WT_WARPS * 32, wsm)) != cudaSuccess) \
+        return e;                                                                                        \
+      w_<<<std::max(1, per_sm) * sms, WT_WARPS * 32, wsm, s>>>(queries, dim, dpad, ix->d_entry_rows,    \
+                                                             ix->d_entry_ids, ix->d_offsets, q_offs, q_list, \
+                                                             task_offs, coarse, np, part_d, part_i);    \
+      merge_starts_kernel<NS><<<(nq + 255) / 256, 256, 0, s>>>(part_d, part_i, nq, np, ns, out);         \
+      break;                                                                                             \
+    }                                                                                                    \
     auto k_ = clusters_tiled_kernel<M, NS>;                                                              \
     if ((e = allow_smem(k_, smem)) != cudaSuccess) return e;                                             \
     k_<<<coarse, ts.warps * 32, smem, s>>>(queries, dim, dpad, ix->d_entry_rows, ix->d_entry_ids,         \
@@ -686,7 +811,7 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
     case SONG_METRIC_IP: SONG_HEADS_BY_NP(SONG_METRIC_IP); break;
     default: SONG_HEADS_BY_NP(SONG_METRIC_COS); break;
   }
-  cluster_scan_kernel<<<1, 1024, 0, s>>>(ix->d_cl_count, coarse, q_offs, cursor);
+  cluster_scan_kernel<<<1, 1024, 0, s>>>(ix->d_cl_count, coarse, q_offs, cursor, task_offs);
   cluster_scatter_kernel<<<static_cast<unsigned>(std::min<size_t>((pairs + 255) / 256, 4096)), 256, 0, s>>>(
       probes, static_cast<int>(pairs), cursor, q_list);
   switch (ix->dx.metric) {

@@ -581,9 +581,17 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
 }
 
 // Small queues (S <= 4, pq < 128) ask for six resident blocks (24 warps per
-// SM): at most 80 registers, and the per-warp shared memory of such pq fits.
+// SM, at most 80 registers; the per-warp shared memory of such pq fits).
+// Measured on the headline search: 5 -> 6 blocks 10 % faster; 8 blocks (64
+// registers) 3 % slower than 6.
+template <int METRIC, int STORAGE, int S, bool LEARNED>
+struct MinBlocks {
+  static constexpr int value = S > 4 ? 1 : 6;
+};
+
 template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
-__global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, S <= 4 ? 6 : 1) search_kernel(const Params p) {
+__global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, (MinBlocks<METRIC, STORAGE, S, LEARNED>::value))
+    search_kernel(const Params p) {
   extern __shared__ __align__(128) uint8_t smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
