@@ -97,6 +97,9 @@ def parse_args():
     p.add_argument("--coarse", type=int, default=2048,
                    help="two-level entry choice: this many of the entries are cluster heads (0: flat)")
     p.add_argument("--probes", type=int, default=4, help="clusters searched per query (two-level choice)")
+    p.add_argument("--multiprobe", default="2,2:1:1,4:1:1,1:2",
+                   help="N_MULTIPROBE[:FINISH_CNT[:DOUBLE_CHECK]] settings measured beside the entries arm, each "
+                        "at the smallest pq reaching --recall ('' to skip)")
     p.add_argument("--serve-rate", type=float, default=20000.0, help="mean offered queries/s (serve)")
     p.add_argument("--serve-seconds", type=float, default=6.0, help="length of each request stream (serve)")
     p.add_argument("--rerank", type=int, default=100, help="FP32 re-ranked candidates (BF16 path)")
@@ -893,6 +896,22 @@ def run_search(args, torch, rank, world, local, dist):
         ent.update({"entries": args.entries, "starts_per_query": args.starts, "coarse": args.coarse,
                     "probes": args.probes, "pq_sweep_recall_qps": sweepe})
         log("[bench] FP32 from entries: %s" % ent)
+    # ---- the reference's N_MULTIPROBE / FINISH_CNT knobs on the entries arm --
+    multi = None
+    if ent and args.multiprobe:
+        multi = []
+        for spec in args.multiprobe.split(","):
+            parts = [int(x) for x in spec.split(":")]
+            P, F, D = parts[0], parts[1] if len(parts) > 1 else 1, parts[2] if len(parts) > 2 else 0
+            ixe.set_multiprobe(P, F, D)
+            pqm, swm = sweep_pq(torch, rune, w, data, queries, kth10, k, args.recall, False,
+                                "fp32+entries probes %d finish %d double-check %d" % (P, F, D))
+            r = measure_arm(torch, rune, pqm, msteps, flush, stream, data, queries, kth10, w)
+            r.update({"n_multiprobe": P, "finish_cnt": F, "double_check": bool(D), "pq_sweep_recall_qps": swm,
+                      "vs_single_probe": round(r["qps"] / ent["qps"], 3)})
+            multi.append(r)
+            log("[bench] multi-probe: %s" % r)
+        ixe.set_multiprobe(1, 1)
     if not args.no_table:
         table, top100 = pq_table(torch, ixe or ix32, dq, stream, flush, data, queries, kth10, kth100, w, args.recall)
 
@@ -1066,6 +1085,7 @@ def run_search(args, torch, rank, world, local, dist):
             else None,
             "top100": top100,
             "pq_table": table,
+            "multi_probe_from_entries": multi,
             "l2": "flushed between steps (256 MB write); index > L2",
             "parallelism": "replicas" if world > 1 else "single GPU"})
         line = {

@@ -175,6 +175,27 @@ int song_index_set_early_exit(song_index *index, const float *weights, float thr
  * coded the same way on every search. */
 int song_index_set_hash_planes(song_index *index, const float *planes);
 
+/* The reference kernel's multi-probe knobs as run-time values (compile-time
+ * macros there; generate_template.sh:17-18 and fill_parameters.sh:36-37 set
+ * the first two).  All at their defaults -- (1, 1, 0), as in the reference --
+ * select the plain search.
+ *   probes (N_MULTIPROBE, warp_astar_accelerator.h:29; 1..SONG_MAX_PROBES):
+ *     vertices popped per iteration; only an iteration's first pop takes the
+ *     finish test, and the unvisited neighbours of all its pops are listed
+ *     before their distances are computed and select-inserted in order
+ *     (:182-322).  A vertex adjacent to two pops is listed twice and, without
+ *     double_check, can enter the queue and the result twice, as in the
+ *     reference.
+ *   finish_cnt (FINISH_CNT, :30; >= 1): the search ends when the finish test
+ *     has held that many times; a pop that passes it before then is expanded
+ *     like any other (:190-197,227).
+ *   double_check (__ENABLE_MULTIPROBE_DOUBLE_CHECK, :307-310; 0 or 1): the
+ *     select-insert skips a candidate already in the visited hash.
+ * F32 storage.  Does not combine with early exit, a hop limit, tracing or a
+ * server: those reject an index with any knob away from its default. */
+#define SONG_MAX_PROBES 4
+int song_index_set_multiprobe(song_index *index, int probes, int finish_cnt, int double_check);
+
 /* Fixed hop budget (0 = off): stop every query after max_hops expansions.
  * A baseline heuristic to compare the learned exit against; no counterpart
  * in the reference.  F32 and BF16 storage. */

@@ -79,10 +79,14 @@ def lib():
         L.orc_kernel_search.argtypes = [P, P, i32, i32, i32, i32, P, P, P, P, i32]
         L.orc_kernel_search_log.restype = i32
         L.orc_kernel_search_log.argtypes = [P, P, i32, i32, i32, P, P, i32, P]
+        L.orc_kernel_search_log_multi.restype = i32
+        L.orc_kernel_search_log_multi.argtypes = [P, P, i32, i32, i32, i32, i32, i32, P, P, i32, P]
         L.orc_classify.restype = i32
         L.orc_classify.argtypes = [P, i32, P, i32, P]
         L.orc_kernel_search_from.restype = i32
         L.orc_kernel_search_from.argtypes = [P, P, i32, P, i32, i32, i32, i32, P, P, P, P, i32]
+        L.orc_kernel_search_multi.restype = i32
+        L.orc_kernel_search_multi.argtypes = [P, P, i32, P, i32, i32, i32, i32, i32, i32, i32, P, P, P, P, i32]
         L.orc_nearest_entry_2level.restype = i32
         L.orc_nearest_entry_2level.argtypes = [P, P, i32, P, i32, i32, i32, i32, i32, P, i32]
         L.orc_nearest_entry.restype = i32
@@ -132,21 +136,31 @@ class OracleIndex:
     def ref(self):
         return ctypes.byref(self._s)
 
-    def kernel_search(self, queries, pq, mode=MODE_LEX, use_fma=True, nthreads=None):
+    def kernel_search(self, queries, pq, mode=MODE_LEX, use_fma=True, nthreads=None, probes=1, finish_cnt=1,
+                      double_check=False):
+        """Batched search from vertex 0.  probes / finish_cnt / double_check
+        are the reference's N_MULTIPROBE / FINISH_CNT (warp_astar_accelerator.h:
+        29-30) and __ENABLE_MULTIPROBE_DOUBLE_CHECK (:307-310)."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         nq = q.shape[0]
         out = np.empty((nq, pq), dtype=np.uint64)
         hops = np.empty(nq, dtype=np.int32)
         evals = np.empty(nq, dtype=np.int32)
         popped = np.empty(nq, dtype=np.int32)
-        rc = lib().orc_kernel_search(self.ref, _ptr(q), nq, pq, mode, int(use_fma), _ptr(out),
-                                     _ptr(hops), _ptr(evals), _ptr(popped),
-                                     nthreads or default_threads())
+        if probes == 1 and finish_cnt == 1 and not double_check:
+            rc = lib().orc_kernel_search(self.ref, _ptr(q), nq, pq, mode, int(use_fma), _ptr(out),
+                                         _ptr(hops), _ptr(evals), _ptr(popped),
+                                         nthreads or default_threads())
+        else:
+            rc = lib().orc_kernel_search_multi(self.ref, _ptr(q), nq, None, 1, pq, int(probes), int(finish_cnt),
+                                               int(double_check), mode, int(use_fma), _ptr(out), _ptr(hops),
+                                               _ptr(evals), _ptr(popped), nthreads or default_threads())
         if rc != 0:
             raise ValueError("orc_kernel_search failed")
         return out, hops, evals, popped
 
-    def kernel_search_from(self, queries, starts, pq, mode=MODE_LEX, use_fma=True, nthreads=None):
+    def kernel_search_from(self, queries, starts, pq, mode=MODE_LEX, use_fma=True, nthreads=None, probes=1,
+                           finish_cnt=1, double_check=False):
         """kernel_search with query i starting from the vertices starts[i]
         (an nq-vector: one start each; nq x ns: ns starts each)."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
@@ -157,8 +171,9 @@ class OracleIndex:
         hops = np.empty(nq, dtype=np.int32)
         evals = np.empty(nq, dtype=np.int32)
         popped = np.empty(nq, dtype=np.int32)
-        rc = lib().orc_kernel_search_from(self.ref, _ptr(q), nq, _ptr(st), ns, pq, mode, int(use_fma), _ptr(out),
-                                          _ptr(hops), _ptr(evals), _ptr(popped), nthreads or default_threads())
+        rc = lib().orc_kernel_search_multi(self.ref, _ptr(q), nq, _ptr(st), ns, pq, int(probes), int(finish_cnt),
+                                           int(double_check), mode, int(use_fma), _ptr(out), _ptr(hops),
+                                           _ptr(evals), _ptr(popped), nthreads or default_threads())
         if rc != 0:
             raise ValueError("orc_kernel_search_from failed")
         return out, hops, evals, popped
@@ -183,13 +198,15 @@ class OracleIndex:
             raise ValueError("orc_nearest_entry_2level failed")
         return out
 
-    def kernel_search_log(self, query, pq, mode, use_fma=True, cap=1 << 18):
+    def kernel_search_log(self, query, pq, mode, use_fma=True, cap=1 << 18, probes=1, finish_cnt=1,
+                          double_check=False):
         q = np.ascontiguousarray(query, dtype=np.float32).reshape(-1)
         out = np.empty(pq, dtype=np.uint64)
         log = np.zeros(cap, dtype=EVENT_DTYPE)
         n = ctypes.c_int(0)
-        rc = lib().orc_kernel_search_log(self.ref, _ptr(q), pq, mode, int(use_fma), _ptr(out),
-                                         _ptr(log), cap, ctypes.byref(n))
+        rc = lib().orc_kernel_search_log_multi(self.ref, _ptr(q), pq, int(probes), int(finish_cnt),
+                                               int(double_check), mode,
+                                               int(use_fma), _ptr(out), _ptr(log), cap, ctypes.byref(n))
         if rc != 0:
             raise ValueError("orc_kernel_search_log failed")
         if n.value > cap:
@@ -317,6 +334,8 @@ def ref_lib(shift: int):
         L.ref_cpu_search.argtypes = [ctypes.c_char_p, ctypes.c_char_p, u64, i32, i32, P, i32, i32, P]
         L.ref_kernel_search.restype = i32
         L.ref_kernel_search.argtypes = [P, P, u64, i32, i32, i32, P, i32, i32, P, P, P, P]
+        L.ref_kernel_search_multi.restype = i32
+        L.ref_kernel_search_multi.argtypes = [P, P, u64, i32, i32, i32, P, i32, i32, i32, i32, i32, P, P, P, P]
         L.ref_fixhash_ops.restype = i32
         L.ref_fixhash_ops.argtypes = [i32, P, P, i32, P]
         L.ref_graph_shift.restype = i32
@@ -358,7 +377,11 @@ def ref_cpu_search(data, graph, shift, metric, queries, k):
     return out
 
 
-def ref_kernel_search(data, graph, shift, metric, queries, pq):
+def ref_kernel_search(data, graph, shift, metric, queries, pq, probes=1, finish_cnt=1, double_check=False):
+    """The kernel's search steps through the reference containers; probes,
+    finish_cnt and double_check are N_MULTIPROBE, FINISH_CNT
+    (warp_astar_accelerator.h:29-30) and __ENABLE_MULTIPROBE_DOUBLE_CHECK
+    (:307-310)."""
     data = np.ascontiguousarray(data, dtype=np.float32)
     graph = np.ascontiguousarray(graph, dtype=np.uint64)
     n, dim = data.shape
@@ -368,8 +391,10 @@ def ref_kernel_search(data, graph, shift, metric, queries, pq):
     hops = np.empty(nq, dtype=np.int32)
     evals = np.empty(nq, dtype=np.int32)
     popped = np.empty(nq, dtype=np.int32)
-    rc = ref_lib(shift).ref_kernel_search(_ptr(data), _ptr(graph), n, dim, shift, metric, _ptr(q),
-                                          nq, pq, _ptr(out), _ptr(hops), _ptr(evals), _ptr(popped))
+    rc = ref_lib(shift).ref_kernel_search_multi(_ptr(data), _ptr(graph), n, dim, shift, metric, _ptr(q),
+                                                nq, pq, int(probes), int(finish_cnt), int(double_check),
+                                                _ptr(out), _ptr(hops),
+                                                _ptr(evals), _ptr(popped))
     if rc != 0:
         raise ValueError("pq %d not instantiated in the reference harness" % pq)
     return out, hops, evals, popped

@@ -115,9 +115,17 @@ float kdist(int metric, int dim, const float *q, const float *x) {
   return 0;
 }
 
+// probes / finish_cnt: the N_MULTIPROBE / FINISH_CNT knobs of
+// warp_astar_accelerator.h:29-30 (both 1 there); dcheck: the
+// __ENABLE_MULTIPROBE_DOUBLE_CHECK switch (:307-310, off there).  An iteration pops up to
+// `probes` vertices (:184), only its first pop takes the finish test, which
+// counts (:190-192) and ends the search at finish_cnt (:196,227); the
+// unvisited neighbours of all the iteration's pops are listed (:211-224)
+// before the distances (:237-287) and the select-insert (:297-322).
 template <int TOPK>
 int kernel_search_one(const float *data, const uint64_t *graph, int dim, int shift, int metric,
-                      const float *qv, uint64_t *out, int *hops_out, int *evals_out) {
+                      const float *qv, uint64_t *out, int *hops_out, int *evals_out, int probes,
+                      int finish_cnt, int dcheck) {
   const int QUEUE_SIZE = TOPK;
   FixHash<int, TOPK * 4 * 2> *pbf = new FixHash<int, TOPK * 4 * 2>();
   std::vector<KP> q(QUEUE_SIZE + 2), topk(TOPK + 1);
@@ -132,27 +140,33 @@ int kernel_search_one(const float *data, const uint64_t *graph, int dim, int shi
     smmh2::insert(q.data(), heap_size, kp);
     pbf->add(0);
   }
+  int finished = 0;
   while (heap_size > 1) {
-    KP now = smmh2::pop_min(q.data(), heap_size);
-    pbf->del(now.second);
-    if (topk_heap_size == TOPK && (topk[0].first <= now.first)) break;
-    ++hops;
-    topk[topk_heap_size++] = now;
-    push_heap(topk.data(), topk.data() + topk_heap_size);
-    pbf->add(now.second);
-    if (topk_heap_size > TOPK) {
-      pbf->del(topk[0].second);
-      pop_heap(topk.data(), topk.data() + topk_heap_size);
-      --topk_heap_size;
-    }
-    uint64_t offset = now.second << shift;
-    int degree = graph[offset];
     index_list.clear();
-    for (int i = 1; i <= degree; ++i) {
-      idx_t idx = graph[offset + i];
-      if (pbf->test(idx)) continue;
-      index_list.push_back(idx);
+    const int current = heap_size - 1;
+    for (int k = 0; k < probes && k < current; ++k) {
+      KP now = smmh2::pop_min(q.data(), heap_size);
+      pbf->del(now.second);
+      if (k == 0 && topk_heap_size == TOPK && (topk[0].first <= now.first)) ++finished;
+      if (finished >= finish_cnt) break;
+      ++hops;
+      topk[topk_heap_size++] = now;
+      push_heap(topk.data(), topk.data() + topk_heap_size);
+      pbf->add(now.second);
+      if (topk_heap_size > TOPK) {
+        pbf->del(topk[0].second);
+        pop_heap(topk.data(), topk.data() + topk_heap_size);
+        --topk_heap_size;
+      }
+      uint64_t offset = now.second << shift;
+      int degree = graph[offset];
+      for (int i = 1; i <= degree; ++i) {
+        idx_t idx = graph[offset + i];
+        if (pbf->test(idx)) continue;
+        index_list.push_back(idx);
+      }
     }
+    if (finished >= finish_cnt) break;
     dist_list.resize(index_list.size());
     for (size_t i = 0; i < index_list.size(); ++i)
       dist_list[i] = kdist(metric, dim, qv, data + index_list[i] * (uint64_t)dim);
@@ -163,6 +177,7 @@ int kernel_search_one(const float *data, const uint64_t *graph, int dim, int shi
       kp.first = d;
       kp.second = index_list[i];
       if (heap_size >= QUEUE_SIZE + 1 && q[2].first < kp.first) continue;
+      if (dcheck && pbf->test(kp.second)) continue;
       smmh2::insert(q.data(), heap_size, kp);
       pbf->add(kp.second);
       if (heap_size >= QUEUE_SIZE + 2) {
@@ -185,8 +200,8 @@ int kernel_search_one(const float *data, const uint64_t *graph, int dim, int shi
 
 template <int P>
 int dispatch(int pq, const float *data, const uint64_t *graph, int dim, int shift, int metric,
-             const float *qv, uint64_t *out, int *h, int *e) {
-  if (pq == P) return kernel_search_one<P>(data, graph, dim, shift, metric, qv, out, h, e);
+             const float *qv, uint64_t *out, int *h, int *e, int probes, int finish_cnt, int dcheck) {
+  if (pq == P) return kernel_search_one<P>(data, graph, dim, shift, metric, qv, out, h, e, probes, finish_cnt, dcheck);
   return -2;
 }
 
@@ -241,17 +256,20 @@ int ref_cpu_search(const char *graph_path, const char *data_path, uint64_t n, in
   return 0;
 }
 
-// Kernel search steps driven through the reference containers.
-int ref_kernel_search(const float *data, const uint64_t *graph, uint64_t n, int dim, int shift,
-                      int metric, const float *queries, int nq, int pq, uint64_t *out,
-                      int32_t *hops, int32_t *evals, int32_t *popped) {
+// Kernel search steps driven through the reference containers, with the
+// N_MULTIPROBE / FINISH_CNT / __ENABLE_MULTIPROBE_DOUBLE_CHECK knobs as
+// run-time values (1, 1, 0: the reference's defaults).
+int ref_kernel_search_multi(const float *data, const uint64_t *graph, uint64_t n, int dim, int shift,
+                            int metric, const float *queries, int nq, int pq, int probes, int finish_cnt,
+                            int dcheck, uint64_t *out, int32_t *hops, int32_t *evals, int32_t *popped) {
   (void)n;
+  if (probes < 1 || finish_cnt < 1) return -1;
   for (int i = 0; i < nq; ++i) {
     int h = 0, e = 0, r = -2;
     const float *qv = queries + (uint64_t)i * dim;
     uint64_t *o = out + (uint64_t)i * pq;
 #define SONG_REF_P(P) \
-  if (r == -2) r = dispatch<P>(pq, data, graph, dim, shift, metric, qv, o, &h, &e);
+  if (r == -2) r = dispatch<P>(pq, data, graph, dim, shift, metric, qv, o, &h, &e, probes, finish_cnt, dcheck);
     SONG_REF_P(2) SONG_REF_P(4) SONG_REF_P(8) SONG_REF_P(10) SONG_REF_P(16) SONG_REF_P(32)
     SONG_REF_P(50) SONG_REF_P(64) SONG_REF_P(100) SONG_REF_P(128) SONG_REF_P(150)
     SONG_REF_P(200) SONG_REF_P(256) SONG_REF_P(300) SONG_REF_P(400)
@@ -262,6 +280,13 @@ int ref_kernel_search(const float *data, const uint64_t *graph, uint64_t n, int 
     if (popped) popped[i] = r;
   }
   return 0;
+}
+
+int ref_kernel_search(const float *data, const uint64_t *graph, uint64_t n, int dim, int shift,
+                      int metric, const float *queries, int nq, int pq, uint64_t *out,
+                      int32_t *hops, int32_t *evals, int32_t *popped) {
+  return ref_kernel_search_multi(data, graph, n, dim, shift, metric, queries, nq, pq, 1, 1, 0, out, hops, evals,
+                                 popped);
 }
 
 // The reference FixHash on its own: ops[i] = 0 add, 1 del, 2 test of keys[i];

@@ -371,8 +371,8 @@ static int kscratch_init(kscratch *s, int pq, int maxdeg, uint64_t n) {
   s->lq = (lk_t *)malloc(sizeof(lk_t) * (size_t)(pq + 3));
   s->lt = (lk_t *)malloc(sizeof(lk_t) * (size_t)(pq + 2));
   s->tab = (int32_t *)malloc(sizeof(int32_t) * (size_t)8 * (size_t)pq);
-  s->cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(maxdeg + 1));
-  s->cdist = (float *)malloc(sizeof(float) * (size_t)(maxdeg + 1));
+  s->cand = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)ORC_MAX_PROBES * (size_t)(maxdeg + 1));
+  s->cdist = (float *)malloc(sizeof(float) * (size_t)ORC_MAX_PROBES * (size_t)(maxdeg + 1));
   s->tmp_out = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)pq);
   return s->cnt && s->q && s->t && s->lq && s->lt && s->tab && s->cand && s->cdist && s->tmp_out ? 0 : -1;
 }
@@ -480,8 +480,18 @@ static void trace_hop(ktrace *tr, const kscratch *s, int qn, int ts, float d0, i
   f[5] = (float)tr->version;
 }
 
-static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *starts, int ns, int pq,
-                       int mode, int use_fma, kscratch *s, uint64_t *out, int32_t *hops_out,
+/* probes: vertices popped per iteration (warp_astar_accelerator.h:29,
+ * 184-232, N_MULTIPROBE; the reference's default is 1).  Only an iteration's
+ * first pop takes the finish test; the neighbours of all its pops are
+ * filtered before any distance is computed, then select-inserted in order.
+ * finish_cnt: the search ends when the finish test has held that many times
+ * (FINISH_CNT, :30,190-197,227; default 1); a pop that passes the test
+ * before then is processed like any other.  dcheck: the select-insert skips
+ * a candidate already in the visited set (__ENABLE_MULTIPROBE_DOUBLE_CHECK,
+ * :307-310; off by default), which keeps a vertex listed by two pops of one
+ * iteration from entering the queue twice. */
+static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *starts, int ns, int pq, int probes,
+                       int finish_cnt, int dcheck, int mode, int use_fma, kscratch *s, uint64_t *out, int32_t *hops_out,
                        int32_t *evals_out, evlog *L, ktrace *tr) {
   const int cap = 8 * pq; /* FixHash<int, TOPK*4*2>, warp_astar_accelerator.h:59-61 */
   const int shift = ix->shift;
@@ -498,6 +508,7 @@ static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *sta
   int qn = 0;         /* LEX: queue length (ts shared) */
   int hops = 0, evals = 0;
   int last_change = 0;
+  int fin = 0; /* finished[cid] */
 
   /* :173 the search starts at vertex 0.  Entry points generalise it: the ns
    * start vertices enter the queue (and the visited set) in order before the
@@ -520,15 +531,17 @@ static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *sta
   evals = ns;
 
   for (;;) {
+    const int avail = mode == ORC_MODE_REF ? hs - 1 : qn; /* :181 while (heap_size > 1) */
+    if (avail <= 0) break;
+    int m = 0, finished = 0;
+    for (int k = 0; k < probes && k < avail; ++k) {
     uint64_t now_id;
     float now_d;
     if (mode == ORC_MODE_REF) {
-      if (hs <= 1) break;
       kp_t now = smmh_pop_min(s->q, &hs);
       now_id = now.id;
       now_d = (float)now.d;
     } else {
-      if (qn <= 0) break;
       lk_t now = s->lq[0];
       memmove(s->lq, s->lq + 1, sizeof(lk_t) * (size_t)(qn - 1));
       --qn;
@@ -537,11 +550,12 @@ static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *sta
     }
     ev(L, ORC_EV_POP, now_id, now_d);
     vs_del(&vs, now_id);
-    /* :191 finish test uses <= */
+    /* :191 finish test uses <=, on an iteration's first pop only (:190) */
     float tmax = mode == ORC_MODE_REF ? (ts > 0 ? (float)s->t[0].d : 0.0f)
                                       : (ts > 0 ? s->lt[ts - 1].d : 0.0f);
-    if (ts == pq && tmax <= now_d) {
+    if (k == 0 && ts == pq && tmax <= now_d && ++fin >= finish_cnt) {
       ev(L, ORC_EV_FINISH, now_id, now_d);
+      finished = 1;
       break;
     }
     ++hops;
@@ -573,15 +587,16 @@ static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *sta
         ev(L, ORC_EV_TEVICT, top.id, top.d);
       }
     }
-    /* :211-224 neighbour filter, row order */
+    /* :211-224 neighbour filter, row order, appended to the iteration's list */
     const uint64_t *grow = ix->graph + (now_id << shift);
     int degree = (int)grow[0];
-    int m = 0;
     for (int i = 1; i <= degree; ++i) {
       uint64_t nb = grow[i];
       if (vs_test(&vs, nb)) continue;
       s->cand[m++] = nb;
     }
+    }
+    if (finished) break;
     /* :237-287 distances */
     for (int i = 0; i < m; ++i) {
       s->cdist[i] = orc_kernel_distance(ix->metric, ix->dim, qv, row(ix, s->cand[i]), use_fma);
@@ -597,6 +612,10 @@ static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *sta
           ev(L, ORC_EV_SKIP, id, d);
           continue;
         }
+        if (dcheck && vs_test(&vs, id)) {
+          ev(L, ORC_EV_SKIP, id, d);
+          continue;
+        }
         kp_t e = {(double)d, id};
         smmh_insert(s->q, &hs, e);
         vs_add(&vs, id);
@@ -609,6 +628,10 @@ static int ksearch_one(const orc_index *ix, const float *qv, const uint64_t *sta
         }
       } else {
         if (qn >= pq && s->lq[qn - 1].d < d) {
+          ev(L, ORC_EV_SKIP, id, d);
+          continue;
+        }
+        if (dcheck && vs_test(&vs, id)) {
           ev(L, ORC_EV_SKIP, id, d);
           continue;
         }
@@ -671,6 +694,7 @@ typedef struct {
   int32_t *explored;
   const uint64_t *starts;
   int ns;
+  int probes, finish_cnt, dcheck;
 } job_t;
 
 static int maxdeg_of(const orc_index *ix) { return (1 << ix->shift) - 1; }
@@ -690,7 +714,8 @@ static void *kworker(void *arg) {
     const uint64_t zero = 0;
     int ts = ksearch_one(j->ix, j->queries + (size_t)i * (size_t)j->ix->dim,
                          j->starts ? j->starts + (size_t)i * (size_t)j->ns : &zero, j->starts ? j->ns : 1,
-                         j->pq, j->mode, j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e, NULL, NULL);
+                         j->pq, j->probes, j->finish_cnt, j->dcheck, j->mode, j->use_fma, &s, j->out + (size_t)i * (size_t)j->pq, &h, &e,
+                         NULL, NULL);
     if (j->hops) j->hops[i] = h;
     if (j->evals) j->evals[i] = e;
     if (j->popped) j->popped[i] = ts;
@@ -729,7 +754,16 @@ int orc_kernel_search(const orc_index *ix, const float *queries, int nq, int pq,
 int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, const uint64_t *starts, int ns,
                            int pq, int mode, int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                            int32_t *popped, int nthreads) {
+  return orc_kernel_search_multi(ix, queries, nq, starts, ns, pq, 1, 1, 0, mode, use_fma, out, hops, evals,
+                                 popped, nthreads);
+}
+
+int orc_kernel_search_multi(const orc_index *ix, const float *queries, int nq, const uint64_t *starts, int ns,
+                            int pq, int probes, int finish_cnt, int double_check, int mode, int use_fma,
+                            uint64_t *out,
+                            int32_t *hops, int32_t *evals, int32_t *popped, int nthreads) {
   if (check_index(ix) || !queries || !out || nq < 0 || pq < 2 || pq > 4095) return -1;
+  if (probes < 1 || probes > ORC_MAX_PROBES || finish_cnt < 1) return -1;
   if (mode != ORC_MODE_REF && mode != ORC_MODE_LEX && mode != ORC_MODE_LEX_EXACT) return -1;
   job_t j;
   memset(&j, 0, sizeof j);
@@ -745,6 +779,9 @@ int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, co
   j.popped = popped;
   j.starts = starts;
   j.ns = ns;
+  j.probes = probes;
+  j.finish_cnt = finish_cnt;
+  j.dcheck = double_check != 0;
   if (starts) {
     if (ns < 1 || ns > pq) return -1;
     for (size_t i = 0; i < (size_t)nq * (size_t)ns; ++i)
@@ -755,7 +792,13 @@ int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, co
 
 int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int mode, int use_fma,
                           uint64_t *out, orc_event *log, int cap, int *n_events) {
+  return orc_kernel_search_log_multi(ix, query, pq, 1, 1, 0, mode, use_fma, out, log, cap, n_events);
+}
+
+int orc_kernel_search_log_multi(const orc_index *ix, const float *query, int pq, int probes, int finish_cnt,
+                                int double_check, int mode, int use_fma, uint64_t *out, orc_event *log, int cap, int *n_events) {
   if (check_index(ix) || !query || !out || pq < 2 || pq > 4095) return -1;
+  if (probes < 1 || probes > ORC_MAX_PROBES || finish_cnt < 1) return -1;
   kscratch s;
   if (kscratch_init(&s, pq, maxdeg_of(ix), ix->n) != 0) {
     kscratch_free(&s);
@@ -763,7 +806,8 @@ int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int m
   }
   evlog L = {log, cap, 0};
   const uint64_t zero = 0;
-  ksearch_one(ix, query, &zero, 1, pq, mode, use_fma, &s, out, NULL, NULL, &L, NULL);
+  ksearch_one(ix, query, &zero, 1, pq, probes, finish_cnt, double_check != 0, mode, use_fma, &s, out, NULL, NULL,
+              &L, NULL);
   if (n_events) *n_events = L.n;
   kscratch_free(&s);
   return 0;
@@ -782,7 +826,7 @@ int orc_kernel_search_trace(const orc_index *ix, const float *query, int pq, int
   }
   ktrace tr = {k, trace_hops, trace, 0, 0};
   const uint64_t zero = 0;
-  ksearch_one(ix, query, &zero, 1, pq, mode, use_fma, &s, out, hops, evals, NULL, &tr);
+  ksearch_one(ix, query, &zero, 1, pq, 1, 1, 0, mode, use_fma, &s, out, hops, evals, NULL, &tr);
   if (final_version) *final_version = tr.version;
   if (traced) *traced = tr.traced;
   kscratch_free(&s);

@@ -105,6 +105,20 @@ int orc_kernel_search_from(const orc_index *ix, const float *queries, int nq, co
                            int pq, int mode, int use_fma, uint64_t *out, int32_t *hops, int32_t *evals,
                            int32_t *popped, int nthreads);
 
+/* orc_kernel_search_from with the reference's search knobs: `probes`
+ * (N_MULTIPROBE, warp_astar_accelerator.h:29; 1..ORC_MAX_PROBES) vertices
+ * popped per iteration -- only an iteration's first pop takes the finish
+ * test, and the neighbours of all its pops are filtered before their
+ * distances are computed and select-inserted in order (:184-232);
+ * `finish_cnt` (FINISH_CNT, :30; >= 1): the search ends when the finish test
+ * has held that many times (:190-197); `double_check`
+ * (__ENABLE_MULTIPROBE_DOUBLE_CHECK, :307-310): the select-insert skips a
+ * candidate already in the visited set. */
+#define ORC_MAX_PROBES 4
+int orc_kernel_search_multi(const orc_index *ix, const float *queries, int nq, const uint64_t *starts, int ns,
+                            int pq, int probes, int finish_cnt, int double_check, int mode, int use_fma,
+                            uint64_t *out, int32_t *hops, int32_t *evals, int32_t *popped, int nthreads);
+
 /* Entry-point choice: starts[i*ns ..] = the ns entries with the smallest
  * kernel distance to query i, ascending by (distance, id). */
 int orc_nearest_entry(const orc_index *ix, const float *queries, int nq, const uint64_t *entries, int ne,
@@ -123,6 +137,8 @@ int orc_nearest_entry_2level(const orc_index *ix, const float *queries, int nq, 
  * number produced, which may exceed cap). */
 int orc_kernel_search_log(const orc_index *ix, const float *query, int pq, int mode, int use_fma,
                           uint64_t *out, orc_event *log, int cap, int *n_events);
+int orc_kernel_search_log_multi(const orc_index *ix, const float *query, int pq, int probes, int finish_cnt,
+                                int double_check, int mode, int use_fma, uint64_t *out, orc_event *log, int cap, int *n_events);
 
 /* One LEX / LEX_EXACT query with the learned search kernel's per-hop trace:
  * for hop h < min(hops, trace_hops), trace[h*ORC_TRACE_FIELDS + 0..4] are the

@@ -44,7 +44,7 @@ EXPORTED = [
     "song_index_free", "song_index_info", "song_search", "song_search_device",
     "song_astar_search_batch", "song_graph_build", "song_graph_build_gpu", "song_index_set_entries", "song_index_set_entries_2level", "song_debug_fixhash", "song_search_noalloc",
     "song_index_set_rerank", "song_index_rows", "song_index_set_early_exit", "song_search_trace_device",
-    "song_index_set_hop_limit", "song_index_set_timing", "song_index_timing", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
+    "song_index_set_hop_limit", "song_index_set_multiprobe", "song_index_set_timing", "song_index_timing", "song_mlp_train_device", "song_mlp_grad", "song_mlp_forward",
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
     "song_index_set_hash_planes",
     "song_server_set_idle_polls", "song_server_running", "song_server_wait", "song_debug_fail_alloc",
@@ -115,6 +115,8 @@ def load_library():
     L.song_search_trace_device.argtypes = [P, P, i32, i32, i32, i32, P, P, P, P, P, P]
     L.song_index_set_hop_limit.restype = i32
     L.song_index_set_hop_limit.argtypes = [P, i32]
+    L.song_index_set_multiprobe.restype = i32
+    L.song_index_set_multiprobe.argtypes = [P, i32, i32, i32]
     L.song_index_set_timing.restype = i32
     L.song_index_set_timing.argtypes = [P, i32]
     L.song_index_timing.restype = i32
@@ -276,6 +278,14 @@ class Index:
     def set_hop_limit(self, max_hops):
         """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""
         _check(load_library().song_index_set_hop_limit(self._h, int(max_hops)))
+
+    def set_multiprobe(self, probes=1, finish_cnt=1, double_check=False):
+        """The reference kernel's N_MULTIPROBE / FINISH_CNT knobs
+        (warp_astar_accelerator.h:29-30) and __ENABLE_MULTIPROBE_DOUBLE_CHECK
+        switch (:307-310) as run-time values; (1, 1, False) is the
+        reference's default search."""
+        _check(load_library().song_index_set_multiprobe(self._h, int(probes), int(finish_cnt),
+                                                        int(bool(double_check))))
 
     def trace_device(self, q_ptr, nq, pq, k, trace_hops, trace_ptr, final_ptr, out_ptr,
                      hops_ptr=None, evals_ptr=None, stream=None):

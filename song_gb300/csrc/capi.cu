@@ -50,7 +50,7 @@ int check_search_args(const song_index *ix, int nq, int pq, int k) {
   if (nq < 0) return fail(SONG_ERR_ARG, "nq must be >= 0");
   if (pq < 2 || pq > SONG_MAX_PQ) return fail(SONG_ERR_ARG, "pq must be in [2, %d]", SONG_MAX_PQ);
   if (k < 1 || k > pq) return fail(SONG_ERR_ARG, "k must be in [1, pq]");
-  uint32_t wb = search_warp_bytes(ix->dx, pq);
+  uint32_t wb = search_warp_bytes(ix->dx, pq, multi_knobs(ix->probes, ix->finish_cnt, ix->double_check));
   if (wb > 227u * 1024u)
     return fail(SONG_ERR_ARG, "pq %d with dim %d needs %u B of shared memory per warp", pq,
                 ix->dx.dim, wb);
@@ -200,6 +200,9 @@ void apply_index_settings(const song_index *ix, SearchCall &c) {
   c.exit_max_hops = ix->max_hops;
   c.wait_limit = ix->wait_limit;
   c.extra_tx = ix->extra_tx;
+  c.probes = ix->probes;
+  c.finish_cnt = ix->finish_cnt;
+  c.double_check = ix->double_check;
 }
 }  // namespace song
 
@@ -501,6 +504,8 @@ int song_index_set_early_exit(song_index *ix, const float *weights, float thresh
   }
   if (every < 1 || min_hops < 0) return fail(SONG_ERR_ARG, "every must be >= 1 and min_hops >= 0");
   if (ix->dx.storage >= SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "early exit is built for F32 and BF16 storage");
+  if (song::multi_knobs(ix->probes, ix->finish_cnt, ix->double_check))
+    return fail(SONG_ERR_ARG, "early exit does not combine with multi-probe search");
   std::vector<__nv_bfloat16> w(SONG_MLP_PARAMS);
   for (int i = 0; i < SONG_MLP_PARAMS; ++i) w[i] = __float2bfloat16_rn(weights[i]);
   if (!ix->d_mlp) {
@@ -541,12 +546,30 @@ int song_index_timing(song_index *ix, float *entry_ms, float *search_ms) {
   return SONG_OK;
 }
 
+int song_index_set_multiprobe(song_index *ix, int probes, int finish_cnt, int double_check) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  if (probes < 1 || probes > SONG_MAX_PROBES || finish_cnt < 1)
+    return fail(SONG_ERR_ARG, "probes must be in [1, %d] and finish_cnt >= 1", SONG_MAX_PROBES);
+  const bool multi = song::multi_knobs(probes, finish_cnt, double_check);
+  if (multi && ix->dx.storage != SONG_STORAGE_F32)
+    return fail(SONG_ERR_ARG, "multi-probe search is built for F32 storage");
+  if (multi && (ix->d_mlp || ix->max_hops > 0))
+    return fail(SONG_ERR_ARG, "multi-probe search does not combine with early exit or a hop limit");
+  ix->probes = probes;
+  ix->finish_cnt = finish_cnt;
+  ix->double_check = double_check != 0;
+  return SONG_OK;
+}
+
 int song_index_set_hop_limit(song_index *ix, int max_hops) {
   g_last_error.clear();
   if (!ix) return fail(SONG_ERR_ARG, "null index");
   if (max_hops < 0) return fail(SONG_ERR_ARG, "max_hops must be >= 0");
   if (max_hops > 0 && ix->dx.storage >= SONG_STORAGE_FP8)
     return fail(SONG_ERR_ARG, "the hop limit is built for F32 and BF16 storage");
+  if (max_hops > 0 && song::multi_knobs(ix->probes, ix->finish_cnt, ix->double_check))
+    return fail(SONG_ERR_ARG, "a hop limit does not combine with multi-probe search");
   ix->max_hops = max_hops;
   return SONG_OK;
 }
@@ -561,6 +584,8 @@ int song_search_trace_device(song_index *ix, const float *d_queries, int nq, int
   if (!d_queries || !d_out || !d_trace || !d_final || trace_hops < 1)
     return fail(SONG_ERR_ARG, "null buffer or trace_hops < 1");
   if (ix->dx.storage >= SONG_STORAGE_FP8) return fail(SONG_ERR_ARG, "tracing is built for F32 and BF16 storage");
+  if (song::multi_knobs(ix->probes, ix->finish_cnt, ix->double_check))
+    return fail(SONG_ERR_ARG, "tracing records the single-probe search: reset the multi-probe knobs first");
   DeviceGuard g(ix->device);
   if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -47,6 +47,9 @@ struct SearchCall {
   const uint32_t *qcodes = nullptr;  // BITS storage: nq x 8 query code words
   uint32_t wait_limit = 1u << 24;  // polls of a bounded mbarrier wait
   uint32_t extra_tx = 0;           // test hook (song_debug_set_wait)
+  int probes = 1;                  // N_MULTIPROBE (song_index_set_multiprobe)
+  int finish_cnt = 1;              // FINISH_CNT
+  int double_check = 0;            // __ENABLE_MULTIPROBE_DOUBLE_CHECK
 };
 
 // Launch the plain search.  Returns a cudaError_t-compatible code (0 ok) or
@@ -54,7 +57,11 @@ struct SearchCall {
 int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t stream);
 
 // Shared-memory bytes one warp needs for (ix, pq).
-uint32_t search_warp_bytes(const DeviceIndex &ix, int pq);
+uint32_t search_warp_bytes(const DeviceIndex &ix, int pq, bool multi = false);
+// Whether an index's knobs select the multi-probe kernel.
+inline bool multi_knobs(int probes, int finish_cnt, int double_check) {
+  return probes > 1 || finish_cnt > 1 || double_check != 0;
+}
 
 int launch_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *out, cudaStream_t s);
 
@@ -113,6 +120,9 @@ struct song_index {
   int max_hops = 0;                 // fixed hop budget, 0 = off
   uint32_t wait_limit = 1u << 24;   // polls of the kernel's bounded waits (song_debug_set_wait)
   uint32_t extra_tx = 0;            // test hook: bytes no copy delivers (song_debug_set_wait)
+  int probes = 1;                   // song_index_set_multiprobe
+  int finish_cnt = 1;
+  int double_check = 0;
   uint32_t *d_counter = nullptr;
   int32_t *d_error = nullptr;
   cudaStream_t stream = nullptr;

@@ -52,7 +52,7 @@ int exact_cap(int pq) {
   return c;
 }
 
-Layout make_layout(const DeviceIndex &ix, int pq, bool learned) {
+Layout make_layout(const DeviceIndex &ix, int pq, bool learned, bool multi = false) {
   Layout L;
   L.H = stage_rows(ix.row_bytes, pq);
   L.S = queue_segment(pq);
@@ -62,7 +62,7 @@ Layout make_layout(const DeviceIndex &ix, int pq, bool learned) {
   L.off_mbar = off;
   off += 16;
   L.off_cand = off;
-  off += 32 * 4;
+  off += (multi ? MAX_PROBES : 1) * 32 * 4;
   off = align_up(off, 16);
   L.off_q = off;
   off += align_up(static_cast<uint32_t>(ix.dim) * 4u, 16);
@@ -121,12 +121,16 @@ int get_shape(const void *fn, uint32_t warp_bytes, uint32_t extra, int *wpb, int
   return 0;
 }
 
-uint32_t search_warp_bytes(const DeviceIndex &ix, int pq) { return make_layout(ix, pq, false).warp_bytes; }
+uint32_t search_warp_bytes(const DeviceIndex &ix, int pq, bool multi) {
+  return make_layout(ix, pq, false, multi).warp_bytes;
+}
 
 int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t stream) {
   if (c.nq <= 0) return 0;
   const bool learned = c.mlp != nullptr || c.trace != nullptr || c.exit_max_hops > 0;
-  const Layout L = make_layout(ix, c.pq, learned);
+  const bool multi = c.probes > 1 || c.finish_cnt > 1 || c.double_check;
+  if (multi && (learned || ix.storage != 0 || c.probes > MAX_PROBES || c.finish_cnt < 1)) return -1;
+  const Layout L = make_layout(ix, c.pq, learned, multi);
   Params p;
   p.rows = static_cast<const uint8_t *>(ix.rows);
   p.row_bytes = ix.row_bytes;
@@ -168,6 +172,10 @@ int launch_search(const DeviceIndex &ix, const SearchCall &c, cudaStream_t strea
   p.qcodes = c.qcodes;
   p.wait_limit = c.wait_limit;
   p.extra_tx = c.extra_tx;
+  p.probes = c.probes;
+  p.finish_cnt = c.finish_cnt;
+  p.double_check = c.double_check;
+  if (multi) return launch_multi(p, ix.metric, L.H, L.S, stream);
   if (learned) {
     if (ix.storage >= 2) return -1;
     return launch_learned(p, ix.storage, ix.metric, L.H, L.S, stream);

@@ -41,6 +41,7 @@
 namespace song {
 
 constexpr int MAX_WARPS_PER_BLOCK = 4;
+constexpr int MAX_PROBES = 4;  // candidate list of the MULTI kernel: MAX_PROBES * 32 ids
 constexpr int MLP_IN = 5, MLP_H = 32;
 // FP32 parameters of the early-exit network, in this order.
 constexpr int MLP_W1 = 0;                        // [MLP_H][MLP_IN]
@@ -76,6 +77,10 @@ struct Params {
   int log2cap;     // ExactVisited (learned kernel)
   uint32_t wait_limit;  // polls of a bounded mbarrier wait
   uint32_t extra_tx;    // test hook: bytes every copy batch expects beyond its rows (0 in use)
+  // the reference's N_MULTIPROBE / FINISH_CNT knobs (MULTI kernel only)
+  int probes;      // vertices popped per iteration, 1..MAX_PROBES
+  int finish_cnt;  // finish tests that must hold before the search ends, >= 1
+  int double_check;  // select-insert skips candidates already visited (__ENABLE_MULTIPROBE_DOUBLE_CHECK)
   // learned variant
   const __nv_bfloat16 *mlp;  // MLP_NPARAM weights (BF16), null = no early exit
   float exit_threshold;
@@ -362,8 +367,9 @@ struct QueryStats {
 // One query: the search of warp_astar_accelerator.h:111-335 with the query
 // vector at qsrc, queue bound pq, k ids written ascending to o.  `trace`
 // (LEARNED) receives the per-hop features or is null.  False if a bulk copy
-// never completed.
-template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
+// never completed.  MULTI: the reference's N_MULTIPROBE / FINISH_CNT knobs
+// (p.probes, p.finish_cnt) as run-time values.
+template <int METRIC, int STORAGE, int H, int S, bool LEARNED, bool MULTI = false>
 __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const float *qsrc, const uint32_t *starts,
                                           int ns, int pq, int k, uint64_t *o, float *trace, QueryStats &st,
                                           int lane, const uint32_t *qcode = nullptr) {
@@ -419,7 +425,110 @@ __device__ __forceinline__ bool run_query(const Params &p, WarpCtx &w, const flo
   int last_change = 0;       // hop of the latest change (LEARNED)
   uint64_t kth_key = ~0ull;  // k-th smallest key of T, ~0 while tn < k (LEARNED)
 
+  int finished = 0;  // MULTI: finish tests that held (finished[cid], :190-192)
   while (qn > 0) {
+    if constexpr (MULTI) {
+      // :182-228 up to p.probes pops per iteration.  Only the first takes the
+      // finish test, which counts; the search ends when p.finish_cnt tests
+      // held.  Every pop goes to the top-pq list, and the unvisited
+      // neighbours of all of them are listed, in pop and row order (a vertex
+      // adjacent to two pops may be listed twice, as in the reference),
+      // before any distance is computed.
+      int m = 0;
+      bool fin = false;
+      const int avail = qn;
+      for (int kp = 0; kp < p.probes && kp < avail; ++kp) {
+        uint64_t qh;
+        const uint64_t now = Q.pop_window(C - pq, lane, &qh);
+        --qn;
+        const uint32_t now_id = key_id(now);
+        const uint32_t a = (kp == 0 && now_id == next_id)
+                               ? a_next
+                               : (lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(now_id) << p.shift) + lane) : 0u);
+        const int now_home = vh.slot(now_id);
+        vh.del_at(now_id, now_home, lane);
+        if (kp == 0 && tn == pq && key_dist(T.max()) <= key_dist(now) && ++finished >= p.finish_cnt) {
+          fin = true;
+          break;
+        }
+        ++hops;
+        // :198-210 a later pop can lie above the list maximum; then it is
+        // the key that leaves (add, then delete, as the reference does).
+        const uint64_t tmax = T.max();
+        const uint64_t ev = now < tmax ? tmax : now;
+        T.insert_evict(now, lane);
+        vh.add_at(now_id, now_home, lane);
+        if (tn < pq) ++tn;
+        else vh.del(key_id(ev), lane);
+        const int deg = static_cast<int>(__shfl_sync(FULL, a, 0));
+        const bool fresh = lane >= 1 && lane <= deg && !vh.test(a);
+        const unsigned fm = __ballot_sync(FULL, fresh);
+        if (fresh) w.cbuf[m + __popc(fm & lanemask_lt())] = a;
+        m += __popc(fm);
+      }
+      if (fin) break;
+      __syncwarp();
+      // :237-322 distances and select-insert, 32 candidates at a time, in
+      // list order (the distances do not depend on the queue, so this is the
+      // reference's all-distances-then-all-inserts order).
+      for (int r0 = 0; r0 < m; r0 += 32) {
+        const int mr = min(32, m - r0);
+        const uint32_t cid = lane < mr ? w.cbuf[r0 + lane] : 0u;
+        if (!gather_distances<METRIC, STORAGE, H>(p, w.stage, w.mbar, w.ph0, w.ph1, w.qv, mr, cid, cd, lane, qc))
+          return false;
+        evals += mr;
+        const uint64_t ck = lane < mr ? make_key(cd, cid) : ~0ull;
+        const int chome = vh.slot(cid);
+        if (p.double_check) {
+          // :297-322 with :307-310: a candidate already in the visited hash
+          // (listed by an earlier pop of this iteration, or twice in one row)
+          // is skipped, so the hash calls interleave with the insertions.
+          for (int c = 0; c < mr; ++c) {
+            const uint64_t key = __shfl_sync(FULL, ck, c);
+            const uint64_t qmax = Q.max();
+            if (key_dist(qmax) < key_dist(key)) continue;
+            const uint32_t id = key_id(key);
+            if (vh.test(id)) continue;
+            const uint64_t ev = key < qmax ? qmax : key;
+            Q.insert_evict(key, lane);
+            if (qn < pq) ++qn;
+            vh.add_at(id, __shfl_sync(FULL, chome, c), lane);
+            if (ev != ~0ull) vh.del(key_id(ev), lane);
+          }
+          __syncwarp();
+          continue;
+        }
+        uint64_t my_ev = ~0ull;
+        unsigned ins = 0u;
+        for (int c = 0; c < mr; ++c) {
+          const uint64_t key = __shfl_sync(FULL, ck, c);
+          const uint64_t qmax = Q.max();
+          if (key_dist(qmax) < key_dist(key)) continue;
+          const uint64_t ev = key < qmax ? qmax : key;
+          Q.insert_evict(key, lane);
+          ins |= 1u << c;
+          if (lane == c) my_ev = ev;
+          if (qn < pq) ++qn;
+        }
+        if (ins) {
+          const int ehome = my_ev != ~0ull ? vh.slot(key_id(my_ev)) : 0;
+          do {
+            const int c = __ffs(ins) - 1;
+            ins &= ins - 1u;
+            vh.add_at(__shfl_sync(FULL, cid, c), __shfl_sync(FULL, chome, c), lane);
+            const uint64_t ev = __shfl_sync(FULL, my_ev, c);
+            if (ev != ~0ull) vh.del_at(key_id(ev), __shfl_sync(FULL, ehome, c), lane);
+          } while (ins);
+        }
+        __syncwarp();
+      }
+      // the next iteration's first pop is the queue head: load its row now
+      if (qn > 0) {
+        next_id = key_id(Q.at(C - pq, lane));
+        a_next = lane < nslots ? __ldg(p.adj + (static_cast<uint64_t>(next_id) << p.shift) + lane) : 0u;
+      }
+      continue;
+    }
     // :186-193 pop the minimum, drop it from the visited hash.
     uint64_t qh;  // queue minimum after the pop
     const uint64_t now = Q.pop_window(C - pq, lane, &qh);
@@ -589,7 +698,7 @@ struct MinBlocks {
   static constexpr int value = S > 4 ? 1 : 6;
 };
 
-template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
+template <int METRIC, int STORAGE, int H, int S, bool LEARNED, bool MULTI = false>
 __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, (MinBlocks<METRIC, STORAGE, S, LEARNED>::value))
     search_kernel(const Params p) {
   extern __shared__ __align__(128) uint8_t smem_raw[];
@@ -627,7 +736,7 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, (MinBlocks<METRIC, S
     float *trace = nullptr;
     if (LEARNED && p.trace) trace = p.trace + static_cast<size_t>(qid) * p.trace_hops * TRACE_FIELDS;
     QueryStats st;
-    if (!run_query<METRIC, STORAGE, H, S, LEARNED>(p, w, p.queries + static_cast<size_t>(qid) * p.dim,
+    if (!run_query<METRIC, STORAGE, H, S, LEARNED, MULTI>(p, w, p.queries + static_cast<size_t>(qid) * p.dim,
                                                    p.starts ? p.starts + static_cast<size_t>(qid) * p.n_starts
                                                             : nullptr,
                                                    p.n_starts, p.pq,
@@ -657,9 +766,9 @@ __global__ void __launch_bounds__(MAX_WARPS_PER_BLOCK * 32, (MinBlocks<METRIC, S
 // that keeps the most warps resident per SM (search.cu).
 int get_shape(const void *fn, uint32_t warp_bytes, uint32_t extra_bytes, int *wpb, int *grid_cap);
 
-template <int METRIC, int STORAGE, int H, int S, bool LEARNED>
+template <int METRIC, int STORAGE, int H, int S, bool LEARNED, bool MULTI = false>
 int launch_kernel(const Params &p, cudaStream_t stream) {
-  auto kern = search_kernel<METRIC, STORAGE, H, S, LEARNED>;
+  auto kern = search_kernel<METRIC, STORAGE, H, S, LEARNED, MULTI>;
   const uint32_t extra = LEARNED ? static_cast<uint32_t>(MLP_NPARAM * sizeof(__nv_bfloat16) + 64) : 0u;
   int wpb = 0, cap = 0;
   int e = get_shape(reinterpret_cast<const void *>(kern), p.warp_bytes, extra, &wpb, &cap);
@@ -672,43 +781,44 @@ int launch_kernel(const Params &p, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-template <int METRIC, int STORAGE, int H, bool LEARNED>
+template <int METRIC, int STORAGE, int H, bool LEARNED, bool MULTI = false>
 int launch_by_s(const Params &p, int S, cudaStream_t s) {
   switch (S) {
-    case 1: return launch_kernel<METRIC, STORAGE, H, 1, LEARNED>(p, s);
-    case 2: return launch_kernel<METRIC, STORAGE, H, 2, LEARNED>(p, s);
-    case 4: return launch_kernel<METRIC, STORAGE, H, 4, LEARNED>(p, s);
-    case 8: return launch_kernel<METRIC, STORAGE, H, 8, LEARNED>(p, s);
-    case 16: return launch_kernel<METRIC, STORAGE, H, 16, LEARNED>(p, s);
-    case 32: return launch_kernel<METRIC, STORAGE, H, 32, LEARNED>(p, s);
+    case 1: return launch_kernel<METRIC, STORAGE, H, 1, LEARNED, MULTI>(p, s);
+    case 2: return launch_kernel<METRIC, STORAGE, H, 2, LEARNED, MULTI>(p, s);
+    case 4: return launch_kernel<METRIC, STORAGE, H, 4, LEARNED, MULTI>(p, s);
+    case 8: return launch_kernel<METRIC, STORAGE, H, 8, LEARNED, MULTI>(p, s);
+    case 16: return launch_kernel<METRIC, STORAGE, H, 16, LEARNED, MULTI>(p, s);
+    case 32: return launch_kernel<METRIC, STORAGE, H, 32, LEARNED, MULTI>(p, s);
     default: return -1;
   }
 }
 
-template <int STORAGE, bool LEARNED>
+template <int STORAGE, bool LEARNED, bool MULTI = false>
 int launch_storage(const Params &p, int metric, int H, int S, cudaStream_t s) {
   const int h = H == 1 ? 0 : (H == 2 ? 1 : (H == 4 ? 2 : -1));
   if (h < 0) return -1;
   switch (metric * 3 + h) {
-    case 0: return launch_by_s<0, STORAGE, 1, LEARNED>(p, S, s);
-    case 1: return launch_by_s<0, STORAGE, 2, LEARNED>(p, S, s);
-    case 2: return launch_by_s<0, STORAGE, 4, LEARNED>(p, S, s);
-    case 3: return launch_by_s<1, STORAGE, 1, LEARNED>(p, S, s);
-    case 4: return launch_by_s<1, STORAGE, 2, LEARNED>(p, S, s);
-    case 5: return launch_by_s<1, STORAGE, 4, LEARNED>(p, S, s);
-    case 6: return launch_by_s<2, STORAGE, 1, LEARNED>(p, S, s);
-    case 7: return launch_by_s<2, STORAGE, 2, LEARNED>(p, S, s);
-    case 8: return launch_by_s<2, STORAGE, 4, LEARNED>(p, S, s);
+    case 0: return launch_by_s<0, STORAGE, 1, LEARNED, MULTI>(p, S, s);
+    case 1: return launch_by_s<0, STORAGE, 2, LEARNED, MULTI>(p, S, s);
+    case 2: return launch_by_s<0, STORAGE, 4, LEARNED, MULTI>(p, S, s);
+    case 3: return launch_by_s<1, STORAGE, 1, LEARNED, MULTI>(p, S, s);
+    case 4: return launch_by_s<1, STORAGE, 2, LEARNED, MULTI>(p, S, s);
+    case 5: return launch_by_s<1, STORAGE, 4, LEARNED, MULTI>(p, S, s);
+    case 6: return launch_by_s<2, STORAGE, 1, LEARNED, MULTI>(p, S, s);
+    case 7: return launch_by_s<2, STORAGE, 2, LEARNED, MULTI>(p, S, s);
+    case 8: return launch_by_s<2, STORAGE, 4, LEARNED, MULTI>(p, S, s);
     default: return -1;
   }
 }
 
 // One per translation unit (search_f32.cu, search_bf16.cu, search_fp8.cu,
-// search_learned.cu).
+// search_bits.cu, search_learned.cu, search_multi.cu).
 int launch_f32(const Params &p, int metric, int H, int S, cudaStream_t s);
 int launch_bf16(const Params &p, int metric, int H, int S, cudaStream_t s);
 int launch_fp8(const Params &p, int metric, int H, int S, cudaStream_t s);
 int launch_bits(const Params &p, int metric, int S, cudaStream_t s);
 int launch_learned(const Params &p, int storage, int metric, int H, int S, cudaStream_t s);
+int launch_multi(const Params &p, int metric, int H, int S, cudaStream_t s);
 
 }  // namespace song

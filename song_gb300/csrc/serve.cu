@@ -364,6 +364,8 @@ int song_server_create(song_index *ix, int max_pq, int max_k, int nslots, int sl
       sm_fraction <= 0.0f || sm_fraction > 1.0f)
     return fail(SONG_ERR_ARG, "bad server limits");
   if (ix->dx.storage != SONG_STORAGE_F32) return fail(SONG_ERR_ARG, "the server is built for F32 storage");
+  if (song::multi_knobs(ix->probes, ix->finish_cnt, ix->double_check))
+    return fail(SONG_ERR_ARG, "the server runs the single-probe search: reset the multi-probe knobs first");
   int prev = -1;
   cudaGetDevice(&prev);
   if (prev != ix->device) cudaSetDevice(ix->device);
@@ -421,6 +423,9 @@ int song_server_create(song_index *ix, int max_pq, int max_k, int nslots, int sl
   p.error = ix->d_error;
   p.wait_limit = ix->wait_limit;
   p.extra_tx = ix->extra_tx;
+  p.probes = 1;
+  p.finish_cnt = 1;
+  p.double_check = 0;
   p.n_starts = 1;
   if (ix->n_entries > 0) {  // the index's entry points, fixed for the server's life
     p.entry_rows = ix->d_entry_rows;

@@ -2,14 +2,16 @@
 
 Run in the development container, where the reference tree is readable:
 
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py [search fixhash fma multiprobe]
 
 Everything stored as an expected output comes from oracle/_ref, i.e. from the
 reference's own source files compiled where they lie:
   * graphs      -- FixedDegreeGraph::add_vertex (graph.h:149-167), sequential
                    insertion, dumped by its own dump()
   * kernel ids  -- the search steps of warp_astar_accelerator.h:111-335 driven
-                   through the reference's smmh2.h / bin_heap.h / fixhash.h
+                   through the reference's smmh2.h / bin_heap.h / fixhash.h,
+                   with its N_MULTIPROBE / FINISH_CNT knobs (:29-30) at their
+                   defaults and, in search_multiprobe.npz, away from them
   * CPU ids     -- FixedDegreeGraph::astar_multi_start_search (graph.h:169-216)
   * hash ops    -- FixHash<int, 8*pq> (fixhash.h) add/del/test answers
 Inputs are seeded synthetic vectors (song_gb300.datasets.mixture).  The GPU
@@ -132,16 +134,50 @@ def make_fma_probe():
                         fma_ids=np.array(fma_ids), nofma_ids=np.array(nofma_ids))
 
 
+# (probes, finish_cnt, double_check): the N_MULTIPROBE / FINISH_CNT knobs of
+# warp_astar_accelerator.h:29-30 and its __ENABLE_MULTIPROBE_DOUBLE_CHECK
+# switch (:307-310) away from their defaults (1, 1, off).
+MULTI_KNOBS = ((2, 1, 0), (4, 1, 0), (1, 2, 0), (3, 3, 0), (2, 1, 1), (4, 2, 1))
+MULTI_CASES = ("cos_s4_d16", "l2_s5_d32")
+
+
+def make_multiprobe_case():
+    """Kernel search results with multi-probe / finish-count knobs, on the
+    graphs and queries of two search fixtures (read back from their files)."""
+    out = {}
+    for name in MULTI_CASES:
+        z = np.load(os.path.join(HERE, "search_%s.npz" % name))
+        graph = z["graph"].astype(np.uint64)
+        for probes, fc, dc in MULTI_KNOBS:
+            for pq in PQS:
+                ids, hops, evals, popped = O.ref_kernel_search(z["data"], graph, int(z["shift"]), int(z["metric"]),
+                                                               z["queries"], pq, probes, fc, dc)
+                key = "%s_p%d_f%d_d%d_%d" % (name, probes, fc, dc, pq)
+                out["ids_" + key] = ids
+                out["hops_" + key] = hops
+                out["evals_" + key] = evals
+                out["popped_" + key] = popped
+    out["knobs"] = np.array(MULTI_KNOBS, np.int32)
+    np.savez_compressed(os.path.join(HERE, "search_multiprobe.npz"), **out)
+
+
 def main():
     if not O.ref_available(4) or not O.ref_available(5):
         raise SystemExit("oracle/_ref not built: run bash oracle/build_ref.sh first")
-    for case in CASES:
-        make_search_case(*case)
-        print("wrote search_%s.npz" % case[0])
-    make_fixhash_case()
-    print("wrote fixhash_ops.npz")
-    make_fma_probe()
-    print("wrote fma_probe.npz")
+    only = sys.argv[1:]
+    if not only or "search" in only:
+        for case in CASES:
+            make_search_case(*case)
+            print("wrote search_%s.npz" % case[0])
+    if not only or "fixhash" in only:
+        make_fixhash_case()
+        print("wrote fixhash_ops.npz")
+    if not only or "fma" in only:
+        make_fma_probe()
+        print("wrote fma_probe.npz")
+    if not only or "multiprobe" in only:
+        make_multiprobe_case()
+        print("wrote search_multiprobe.npz")
 
 
 if __name__ == "__main__":

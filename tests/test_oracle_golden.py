@@ -188,3 +188,40 @@ def test_oracle_builder_batches_equal_the_product_builder(oracle, song, name, n,
     a = oracle.graph_build(*args, batch_div=div, nthreads=4)
     b = song.graph_build(*args, batch_div=div, nthreads=4)
     assert np.array_equal(a, b)
+
+
+def test_ref_mode_matches_reference_multiprobe_steps(oracle):
+    """The N_MULTIPROBE / FINISH_CNT knobs (warp_astar_accelerator.h:29-30,
+    184-232) and the double-check switch (:307-310) away from their defaults:
+    REF mode against the reference containers' results."""
+    z = np.load(GOLDEN + "/search_multiprobe.npz")
+    for name in ("cos_s4_d16", "l2_s5_d32"):
+        g = load_golden(name)
+        ix = oracle.OracleIndex(g["data"], g["graph"], int(g["shift"]), int(g["metric"]))
+        for probes, fc, dc in z["knobs"]:
+            for pq in g["pqs"]:
+                key = "%s_p%d_f%d_d%d_%d" % (name, probes, fc, dc, pq)
+                ids, hops, evals, popped = ix.kernel_search(g["queries"], int(pq), oracle.MODE_REF,
+                                                            probes=int(probes), finish_cnt=int(fc),
+                                                            double_check=bool(dc))
+                assert np.array_equal(ids, z["ids_" + key]), key
+                assert np.array_equal(hops, z["hops_" + key]), key
+                assert np.array_equal(evals, z["evals_" + key]), key
+                assert np.array_equal(popped, z["popped_" + key]), key
+
+
+def test_lex_mode_multiprobe_differs_only_by_ties(oracle):
+    z = np.load(GOLDEN + "/search_multiprobe.npz")
+    for name in ("cos_s4_d16", "l2_s5_d32"):
+        g = load_golden(name)
+        ix = oracle.OracleIndex(g["data"], g["graph"], int(g["shift"]), int(g["metric"]))
+        for probes, fc, dc in z["knobs"]:
+            kw = dict(probes=int(probes), finish_cnt=int(fc), double_check=bool(dc))
+            for pq in g["pqs"]:
+                lex, *_ = ix.kernel_search(g["queries"], int(pq), oracle.MODE_LEX, **kw)
+                ref = z["ids_%s_p%d_f%d_d%d_%d" % (name, probes, fc, dc, pq)]
+                for i in np.nonzero((lex != ref).any(axis=1))[0]:
+                    _, la = ix.kernel_search_log(g["queries"][i], int(pq), oracle.MODE_REF, **kw)
+                    _, lb = ix.kernel_search_log(g["queries"][i], int(pq), oracle.MODE_LEX, **kw)
+                    cls, at = oracle.classify(la, lb)
+                    assert cls == 1, "%s %s pq %d query %d parts without a tie" % (name, kw, pq, i)
