@@ -329,6 +329,24 @@ int song_debug_fail_alloc(int n);
 int song_debug_set_wait(song_index *index, uint32_t wait_limit, uint32_t extra_tx);
 int song_debug_server_hold(song_server *server, int hold);
 
+/* Head phase of the two-level entry choice (song_index_set_entries_2level).
+ * By default it scores queries against the coarse entries with a TF32
+ * tensor-core product and re-scores, with the search's exact arithmetic, the
+ * shortlist whose error intervals reach the probes-th best -- the same
+ * clusters as an exact scan.  song_debug_head_path(index, 0) switches to the
+ * exact CUDA-core scan of every coarse entry (1: back); *prepared (may be
+ * NULL) tells whether the tensor path exists for the index (it needs
+ * dim % 4 == 0).  song_debug_head_stats(index, enable, stats): with enable,
+ * later searches count [0] queries, [1] coarse entries re-scored exactly,
+ * [2] queries whose shortlist overflowed into a full scan; stats (3 values,
+ * may be NULL) receives the counts since the previous call, which restart at
+ * zero.  song_debug_head_scores: the tensor-core scores alone, d_scores[q*ld
+ * + h] = approximate dot product of query q and coarse entry h (device
+ * buffers; ld >= the coarse entries, a multiple of 4). */
+int song_debug_head_path(song_index *index, int use_tensor_cores, int *prepared);
+int song_debug_head_stats(song_index *index, int enable, unsigned long long *stats);
+int song_debug_head_scores(song_index *index, const float *d_queries, int nq, float *d_scores, int ld);
+
 /* The visited-hash slot function of the reference's default build
  * (fixhash.h:20-24) evaluated on the device for `count` ids, for tests. */
 int song_debug_fixhash(const uint32_t *ids, int count, int pq, int32_t *slots_out);

@@ -48,7 +48,8 @@ EXPORTED = [
     "song_server_create", "song_server_submit", "song_server_poll", "song_server_result", "song_server_destroy",
     "song_index_set_hash_planes",
     "song_server_set_idle_polls", "song_server_running", "song_server_wait", "song_debug_fail_alloc",
-    "song_debug_set_wait", "song_debug_server_hold",
+    "song_debug_set_wait", "song_debug_server_hold", "song_debug_head_path", "song_debug_head_stats",
+    "song_debug_head_scores",
 ]
 MLP_PARAMS = 1281
 TRACE_FIELDS = 6
@@ -115,6 +116,12 @@ def load_library():
     L.song_search_trace_device.argtypes = [P, P, i32, i32, i32, i32, P, P, P, P, P, P]
     L.song_index_set_hop_limit.restype = i32
     L.song_index_set_hop_limit.argtypes = [P, i32]
+    L.song_debug_head_path.restype = i32
+    L.song_debug_head_path.argtypes = [P, i32, ctypes.POINTER(i32)]
+    L.song_debug_head_stats.restype = i32
+    L.song_debug_head_stats.argtypes = [P, i32, P]
+    L.song_debug_head_scores.restype = i32
+    L.song_debug_head_scores.argtypes = [P, P, i32, P, i32]
     L.song_index_set_multiprobe.restype = i32
     L.song_index_set_multiprobe.argtypes = [P, i32, i32, i32]
     L.song_index_set_timing.restype = i32
@@ -278,6 +285,27 @@ class Index:
     def set_hop_limit(self, max_hops):
         """Fixed hop budget (0 = off), the heuristic the learned exit is compared with."""
         _check(load_library().song_index_set_hop_limit(self._h, int(max_hops)))
+
+    def debug_head_path(self, use_tensor_cores=True):
+        """Head phase of the two-level entry choice: tensor-core shortlist
+        (default) or the exact CUDA-core scan; returns whether the tensor
+        path is prepared for this index."""
+        prepared = ctypes.c_int(0)
+        _check(load_library().song_debug_head_path(self._h, int(bool(use_tensor_cores)), ctypes.byref(prepared)))
+        return bool(prepared.value)
+
+    def debug_head_stats(self, enable=True):
+        """Counts since the previous call: (queries, coarse entries re-scored
+        exactly, shortlist overflows); enable keeps counting."""
+        st = np.zeros(3, dtype=np.uint64)
+        _check(load_library().song_debug_head_stats(self._h, int(bool(enable)), st.ctypes.data_as(ctypes.c_void_p)))
+        return tuple(int(x) for x in st)
+
+    def debug_head_scores(self, q_ptr, nq, scores_ptr, ld):
+        """Tensor-core approximate dot products of nq device queries with the
+        coarse entries into a device buffer (nq x ld floats)."""
+        _check(load_library().song_debug_head_scores(self._h, ctypes.c_void_p(q_ptr), int(nq),
+                                                     ctypes.c_void_p(scores_ptr), int(ld)))
 
     def set_multiprobe(self, probes=1, finish_cnt=1, double_check=False):
         """The reference kernel's N_MULTIPROBE / FINISH_CNT knobs

@@ -22,7 +22,7 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(LIB_DIR, "libsong_gb300.so")
 CLI_PATH = os.path.join(LIB_DIR, "song")
 
-CUDA_SOURCES = ["search.cu", "search_f32.cu", "search_bf16.cu", "search_fp8.cu", "search_bits.cu", "search_learned.cu", "search_multi.cu",
+CUDA_SOURCES = ["search.cu", "search_f32.cu", "search_bf16.cu", "search_fp8.cu", "search_bits.cu", "search_learned.cu", "search_multi.cu", "head_mma.cu",
                 "capi.cu", "noalloc.cu", "mlp.cu", "serve.cu", "graph_build_gpu.cu", "entries.cu"]
 CXX_SOURCES = ["graph_build.cpp"]
 HEADERS = ["device_common.cuh", "internal.h", "reg_queue.cuh", "search_kernel.cuh", "graph_build.h",

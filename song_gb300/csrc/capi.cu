@@ -108,6 +108,9 @@ void release(song_index *ix) {
   cudaFree(ix->d_starts);
   cudaFree(ix->d_planes);
   cudaFree(ix->d_qcodes);
+  cudaFree(ix->d_head_n2);
+  cudaFree(ix->d_head_scores);
+  cudaFree(ix->d_head_stats);
   for (cudaEvent_t &e : ix->ev)
     if (e) cudaEventDestroy(e);
   if (ix->stream) cudaStreamDestroy(ix->stream);
@@ -137,10 +140,11 @@ int launch(song_index *ix, const float *d_q, int nq, int pq, int k, uint64_t *d_
     if (e != 0) return fail(SONG_ERR_CUDA, "query codes: %s", cudaGetErrorString((cudaError_t)e));
     c.qcodes = ix->d_qcodes;
   }
+  // the error flag collects the bounded waits of the entry choice and of the search
+  SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
   if (ix->timing) SONG_CUDA(cudaEventRecord(ix->ev[0], s));
   int rc = song::prepare_starts(ix, c, s);
   if (rc != SONG_OK) return rc;
-  SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), s));
   if (ix->timing) {
     SONG_CUDA(cudaEventRecord(ix->ev[1], s));
     ix->timed_entries = c.starts != nullptr;
@@ -456,6 +460,55 @@ int song_debug_set_wait(song_index *ix, uint32_t wait_limit, uint32_t extra_tx) 
   if (extra_tx % 16 != 0 || extra_tx > (1u << 16)) return fail(SONG_ERR_ARG, "extra_tx must be a multiple of 16, <= 65536");
   ix->wait_limit = wait_limit;
   ix->extra_tx = extra_tx;
+  return SONG_OK;
+}
+
+int song_debug_head_path(song_index *ix, int use_tensor_cores, int *prepared) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  ix->heads_mma_enabled = use_tensor_cores != 0;
+  if (prepared) *prepared = ix->heads_mma ? 1 : 0;
+  return SONG_OK;
+}
+
+int song_debug_head_stats(song_index *ix, int enable, unsigned long long *stats) {
+  g_last_error.clear();
+  if (!ix) return fail(SONG_ERR_ARG, "null index");
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  if (enable && !ix->d_head_stats) {
+    SONG_CUDA(song::dev_malloc(reinterpret_cast<void **>(&ix->d_head_stats), 3 * sizeof(unsigned long long)));
+    SONG_CUDA(cudaMemset(ix->d_head_stats, 0, 3 * sizeof(unsigned long long)));
+  }
+  if (stats) {
+    stats[0] = stats[1] = stats[2] = 0;
+    if (ix->d_head_stats) {
+      SONG_CUDA(cudaStreamSynchronize(ix->stream));
+      SONG_CUDA(cudaDeviceSynchronize());
+      SONG_CUDA(cudaMemcpy(stats, ix->d_head_stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+      SONG_CUDA(cudaMemset(ix->d_head_stats, 0, 3 * sizeof(unsigned long long)));
+    }
+  }
+  ix->head_stats_on = enable != 0;
+  return SONG_OK;
+}
+
+int song_debug_head_scores(song_index *ix, const float *d_queries, int nq, float *d_scores, int ld) {
+  g_last_error.clear();
+  if (!ix || nq < 0 || (nq > 0 && (!d_queries || !d_scores))) return fail(SONG_ERR_ARG, "bad arguments");
+  if (!ix->heads_mma) return fail(SONG_ERR_ARG, "no tensor-core head phase on this index");
+  if (ld < ix->n_coarse || ld % 4 != 0) return fail(SONG_ERR_ARG, "ld must be >= the coarse entries and a multiple of 4");
+  if (nq == 0) return SONG_OK;
+  DeviceGuard g(ix->device);
+  if (!g.ok) return fail(SONG_ERR_CUDA, "cannot select device %d", ix->device);
+  SONG_CUDA(cudaMemsetAsync(ix->d_error, 0, sizeof(int32_t), ix->stream));
+  cudaError_t e = song::launch_head_scores_only(ix, d_queries, nq, d_scores, ld, ix->stream);
+  if (e == cudaErrorInvalidValue) return fail(SONG_ERR_ARG, "queries must be 16-byte aligned");
+  SONG_CUDA(e);
+  SONG_CUDA(cudaStreamSynchronize(ix->stream));
+  int32_t err = 0;
+  SONG_CUDA(cudaMemcpy(&err, ix->d_error, sizeof err, cudaMemcpyDeviceToHost));
+  if (err) return fail(SONG_ERR_CUDA, "a bulk copy or the matrix multiply never completed (bounded wait)");
   return SONG_OK;
 }
 

@@ -483,6 +483,7 @@ __global__ void __launch_bounds__(256) heads_tiled_kernel(const float *queries, 
     float wd;
     uint32_t wid;
     group8_take<NP>(pd, pi, h, wd, wid);
+    if (wid >= static_cast<uint32_t>(n_coarse)) wid = 0;  // no finite distance (a query that is not finite)
     if ((lane & 7) == 0 && q < nq) {
       probe_out[static_cast<size_t>(q) * probes + r] = wid;
       atomicAdd(cl_count + wid, 1u);
@@ -806,10 +807,14 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
     case 4: SONG_CLUSTERS(M, 4); break;   \
     default: SONG_CLUSTERS(M, 8); break;  \
   }
-  switch (ix->dx.metric) {
-    case SONG_METRIC_L2: SONG_HEADS_BY_NP(SONG_METRIC_L2); break;
-    case SONG_METRIC_IP: SONG_HEADS_BY_NP(SONG_METRIC_IP); break;
-    default: SONG_HEADS_BY_NP(SONG_METRIC_COS); break;
+  if (heads_mma_usable(ix, queries, np)) {  // tensor-core scores, exact re-scoring of a shortlist
+    if ((e = launch_heads_mma(ix, queries, nq, np, probes, s)) != cudaSuccess) return e;
+  } else {
+    switch (ix->dx.metric) {
+      case SONG_METRIC_L2: SONG_HEADS_BY_NP(SONG_METRIC_L2); break;
+      case SONG_METRIC_IP: SONG_HEADS_BY_NP(SONG_METRIC_IP); break;
+      default: SONG_HEADS_BY_NP(SONG_METRIC_COS); break;
+    }
   }
   cluster_scan_kernel<<<1, 1024, 0, s>>>(ix->d_cl_count, coarse, q_offs, cursor, task_offs);
   cluster_scatter_kernel<<<static_cast<unsigned>(std::min<size_t>((pairs + 255) / 256, 4096)), 256, 0, s>>>(
@@ -835,6 +840,12 @@ void clear_entries(song_index *ix) {
   cudaFree(ix->d_offsets);
   cudaFree(ix->d_cl_count);
   cudaFree(ix->d_entry_work);
+  cudaFree(ix->d_head_n2);
+  cudaFree(ix->d_head_scores);
+  ix->d_head_n2 = nullptr;
+  ix->d_head_scores = nullptr;
+  ix->cap_head_scores = 0;
+  ix->heads_mma = false;
   ix->d_entry_ids = nullptr;
   ix->d_entry_rows = nullptr;
   ix->d_coarse_rows = nullptr;
@@ -1035,8 +1046,11 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
                                                          ix->d_coarse_rows);
     e = cudaGetLastError();
   }
-  // 4. the per-cluster probe counters of the second kernel
+  // 4. the per-cluster probe counters of the second kernel; the head rows'
+  // tensor map and norms (the tensor-core head phase; without them the
+  // CUDA-core kernel scores the heads)
   if (e == cudaSuccess) e = song::dev_malloc(&ix->d_cl_count, sizeof(uint32_t) * coarse);
+  if (e == cudaSuccess) song::heads_mma_prepare(ix, coarse);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
   cudaFree(d_ids);
   cudaFree(d_rows);

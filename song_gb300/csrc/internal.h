@@ -74,6 +74,17 @@ int launch_hash_codes(const float *rows, uint64_t n, int stride, int dim, const 
 struct song_index;
 
 namespace song {
+// Head phase of the two-level entry choice on the tensor cores (head_mma.cu).
+bool heads_mma_prepare(song_index *ix, int coarse);
+bool heads_mma_usable(const song_index *ix, const float *queries, int np);
+cudaError_t launch_heads_mma(song_index *ix, const float *queries, int nq, int np, uint32_t *probe_out,
+                             cudaStream_t s);
+cudaError_t launch_head_scores_only(song_index *ix, const float *queries, int nq, float *scores, int ld,
+                                    cudaStream_t s);
+
+}  // namespace song
+
+namespace song {
 // Makes `dev` current for the scope and restores the caller's device.
 struct DeviceGuard {
   int prev = -1;
@@ -146,6 +157,16 @@ struct song_index {
   float *d_coarse_rows = nullptr;
   uint32_t *d_offsets = nullptr;
   uint32_t *d_cl_count = nullptr;      // probes per cluster (per call)
+  // head phase on the tensor cores (head_mma.cu): tensor map of the coarse
+  // rows (a CUtensorMap), their squared norms, the per-chunk score buffer
+  unsigned char head_map[128] = {};
+  bool heads_mma = false;              // prepared for this index
+  bool heads_mma_enabled = true;       // song_debug_head_path
+  float *d_head_n2 = nullptr;
+  float *d_head_scores = nullptr;
+  size_t cap_head_scores = 0;
+  bool head_stats_on = false;          // song_debug_head_stats
+  unsigned long long *d_head_stats = nullptr;
   uint32_t *d_entry_work = nullptr;    // per-call lists of the two-level choice
   size_t cap_entry_work = 0;
   int servers = 0;  // servers using the entries (song_server_create); they stay fixed meanwhile
