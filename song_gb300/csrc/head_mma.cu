@@ -9,8 +9,8 @@
 //  1. head_scores_kernel: s~ = q . x for all pairs, a TF32 tcgen05.mma GEMM
 //     (FP32 accumulators in tensor memory).  128 x 128 tiles; the operands are
 //     staged by TMA (cp.async.bulk.tensor.2d) as 128-byte-swizzled K-major
-//     slabs of 32 floats, four slabs in flight; one thread issues the copies
-//     and the MMAs.  In the epilogue each thread reads its query's row of
+//     slabs of 32 floats, two slab pairs in flight; one thread issues the
+//     copies and the MMAs.  In the epilogue each thread reads its query's row of
 //     the accumulators (tcgen05.ld) and turns every score into an interval
 //     [lo, hi] that provably holds the exact search distance (the TF32 error
 //     bound below); it writes the lower bounds and the tile's `probes`
@@ -46,7 +46,8 @@ namespace {
 
 constexpr int HM_B = 128;     // queries (M) and heads (N) per tile
 constexpr int HM_K = 32;      // floats per K slab: one 128-byte swizzle row
-constexpr int HM_STAGES = 4;  // slabs in flight
+constexpr int HM_STAGES = 2;  // slab pairs in flight (67 KB of shared memory: three blocks per SM overlap
+                              // one another's copies, products and epilogues)
 constexpr uint32_t HM_SLAB = HM_B * HM_K * 4;  // 16 KB
 // slabs, then barriers (128 B), then the tile's head norms (2 x 128 floats)
 constexpr size_t HM_SMEM = 1024 + static_cast<size_t>(HM_STAGES) * 2 * HM_SLAB + 128 + 2 * HM_B * 4;
