@@ -73,6 +73,29 @@ def test_tensor_shortlist_equals_exact_scan_and_oracle(song, oracle, dim, metric
     assert np.array_equal(ids, o_ids) and np.array_equal(hops, o_hops) and np.array_equal(evals, o_evals)
 
 
+@pytest.mark.parametrize("dim,metric", [(128, 0), (64, 2), (256, 1)])
+def test_large_clusters_many_queries(song, oracle, dim, metric):
+    """16 clusters of ~250 entries probed by ~500 queries each: many warp
+    tasks per cluster, several row buffers per task; the same starts as the
+    oracle with either head phase."""
+    data, q, graph = _case(song, 6000, dim, metric, 2000, seed=dim + metric + 100)
+    ox = oracle.OracleIndex(data, graph, 5, metric)
+    rng = np.random.default_rng(dim + 1)
+    ent = rng.choice(len(data), 4000, replace=False).astype(np.uint64)
+    coarse, probes, ns = 16, 4, 4
+    starts = ox.nearest_entry_2level(q, ent, coarse, probes, ns)
+    o_ids, o_hops, o_evals, _ = ox.kernel_search_from(q, starts, 30, oracle.MODE_LEX)
+    with song.Index(graph, data, 5, metric) as ix:
+        ix.set_entries(ent, starts=ns, coarse=coarse, probes=probes)
+        assert ix.debug_head_path(True)
+        got = ix.search(q, 30, 30, stats=True)
+        ix.debug_head_path(False)
+        ref = ix.search(q, 30, 30, stats=True)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    assert np.array_equal(got[0], o_ids) and np.array_equal(got[1], o_hops) and np.array_equal(got[2], o_evals)
+
+
 def test_batch_spanning_several_score_chunks(song, oracle):
     """2048 coarse entries: a chunk holds 4096 queries' scores, so 9000
     queries take three chunks (the last one partial)."""
