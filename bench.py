@@ -838,6 +838,22 @@ def pq_table(torch, ix, dq, stream, flush, data, queries, kth10, kth100, w, targ
     return rows, top100
 
 
+def entry_launches(args, w, nq):
+    """Kernels of one entry choice: flat, one; two-level, the query norms and
+    a score + select pair per chunk of queries (tensor-core heads, dims a
+    multiple of 4: a chunk's bounds take at most 32 MB, in 128-query tiles)
+    or one head kernel, then scan, scatter, cluster and merge kernels."""
+    if args.coarse <= 0:
+        return 1
+    if w.dim % 4 == 0:
+        ld = (args.coarse + 3) // 4 * 4
+        chunk = max(128, min((nq + 127) // 128 * 128, (32 << 20) // (4 * ld) // 128 * 128))
+        heads = 1 + 2 * ((nq + chunk - 1) // chunk)
+    else:
+        heads = 1
+    return heads + 4
+
+
 def plain_arm(torch, S, args, w, graph, data, queries, kth10, dq, k, stream, flush, local, msteps):
     t = time.time()
     ix32 = S.Index(graph, data, w.shift, w.metric, device=local)
@@ -902,12 +918,12 @@ def run_search(args, torch, rank, world, local, dist):
         multi = []
         for spec in args.multiprobe.split(","):
             parts = [int(x) for x in spec.split(":")]
-            P, F, D = parts[0], parts[1] if len(parts) > 1 else 1, parts[2] if len(parts) > 2 else 0
-            ixe.set_multiprobe(P, F, D)
+            mp_p, mp_f, mp_d = parts[0], parts[1] if len(parts) > 1 else 1, parts[2] if len(parts) > 2 else 0
+            ixe.set_multiprobe(mp_p, mp_f, mp_d)
             pqm, swm = sweep_pq(torch, rune, w, data, queries, kth10, k, args.recall, False,
-                                "fp32+entries probes %d finish %d double-check %d" % (P, F, D))
+                                "fp32+entries probes %d finish %d double-check %d" % (mp_p, mp_f, mp_d))
             r = measure_arm(torch, rune, pqm, msteps, flush, stream, data, queries, kth10, w)
-            r.update({"n_multiprobe": P, "finish_cnt": F, "double_check": bool(D), "pq_sweep_recall_qps": swm,
+            r.update({"n_multiprobe": mp_p, "finish_cnt": mp_f, "double_check": bool(mp_d), "pq_sweep_recall_qps": swm,
                       "vs_single_probe": round(r["qps"] / ent["qps"], 3)})
             multi.append(r)
             log("[bench] multi-probe: %s" % r)
@@ -1114,7 +1130,7 @@ def run_search(args, torch, rank, world, local, dist):
             "e2e": {"value": round(e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(nq * w.dim * 4),
                     "d2h_bytes_per_step": int(nq * k * 8)},
             "gpu_launches": args.steps * (1 + (0 if mode == "plain" or entries is None
-                                               else (5 if args.coarse > 0 else 1))),
+                                               else entry_launches(args, w, nq))),
             "clocks": clocks,
             "kernel_ms": {"min": round(min(kernel_ms), 4), "median": round(statistics.median(kernel_ms), 4),
                           "max": round(max(kernel_ms), 4)},
