@@ -169,9 +169,11 @@ struct VisitedHash {
     return static_cast<int>(r);
   }
 
+  // s < cap + 32 <= 3 * cap (every caller adds at most 32 to a slot, and
+  // cap = 8 * pq >= 16): two conditional subtractions, no branch
   __device__ __forceinline__ int wrap(int s) const {
-    while (s >= cap) s -= cap;
-    return s;
+    s = s >= cap ? s - cap : s;
+    return s >= cap ? s - cap : s;
   }
 
   __device__ __forceinline__ void clear(int lane) {
