@@ -92,9 +92,9 @@ def parse_args():
                         "without it and a fixed hop budget, from vertex 0 and from entry points); "
                         "precision: storage error and recall table; serve: Poisson request stream; "
                         "build: graph construction, GPU searches vs the CPU builder")
-    p.add_argument("--entries", type=int, default=262144, help="entry vertices of the entries arm (sampled, seeded)")
+    p.add_argument("--entries", type=int, default=524288, help="entry vertices of the entries arm (sampled, seeded)")
     p.add_argument("--starts", type=int, default=4, help="start vertices per query: its nearest entries")
-    p.add_argument("--coarse", type=int, default=2048,
+    p.add_argument("--coarse", type=int, default=4096,
                    help="two-level entry choice: this many of the entries are cluster heads (0: flat)")
     p.add_argument("--probes", type=int, default=4, help="clusters searched per query (two-level choice)")
     p.add_argument("--multiprobe", default="2,2:1:1,4:1:1,1:2",
