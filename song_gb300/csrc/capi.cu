@@ -104,6 +104,7 @@ void release(song_index *ix) {
   cudaFree(ix->d_coarse_rows);
   cudaFree(ix->d_offsets);
   cudaFree(ix->d_cl_count);
+  cudaFree(ix->d_cl_order);
   cudaFree(ix->d_entry_work);
   cudaFree(ix->d_starts);
   cudaFree(ix->d_planes);

@@ -522,16 +522,17 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t s, uint32_t *w
 
 // Exclusive scans of the per-cluster probe counts (one block): offs[0..n],
 // a copy of offs[0..n-1] as the scatter cursors, and task_offs[0..n] of the
-// clusters' warp tasks (one per 4 of its queries).
-__global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *count, int n, uint32_t *offs,
-                                                            uint32_t *cursor, uint32_t *task_offs) {
+// clusters' warp tasks (one per 4 of its queries), the clusters taken in the
+// order `order` (task_offs[i] belongs to cluster order[i]).
+__global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *count, int n, const uint32_t *order,
+                                                            uint32_t *offs, uint32_t *cursor, uint32_t *task_offs) {
   __shared__ uint32_t warp_sum[32];
   const int per = (n + blockDim.x - 1) / blockDim.x;
   const int b = threadIdx.x * per, e = min(n, b + per);
   uint32_t s = 0, st = 0;
   for (int i = b; i < e; ++i) {
     s += count[i];
-    st += (count[i] + 3u) / 4u;
+    st += (count[order[i]] + 3u) / 4u;
   }
   uint32_t total, ttotal;
   uint32_t run = block_exclusive_scan(s, warp_sum, &total);
@@ -541,7 +542,7 @@ __global__ void __launch_bounds__(1024) cluster_scan_kernel(const uint32_t *coun
     cursor[i] = run;
     run += count[i];
     if (task_offs) task_offs[i] = trun;
-    trun += (count[i] + 3u) / 4u;
+    trun += (count[order[i]] + 3u) / 4u;
   }
   if (threadIdx.x == 0) {
     offs[n] = total;
@@ -634,7 +635,8 @@ __global__ void __launch_bounds__(WT_WARPS * 32) clusters_warp_kernel(const floa
                                                                       const uint32_t *fine_ids,
                                                                       const uint32_t *row_offs,
                                                                       const uint32_t *q_offs, const uint32_t *q_list,
-                                                                      const uint32_t *task_offs, int n_clusters,
+                                                                      const uint32_t *task_offs,
+                                                                      const uint32_t *cl_order, int n_clusters,
                                                                       int probes, float *part_d, uint32_t *part_i) {
   extern __shared__ __align__(16) float smt[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -644,15 +646,16 @@ __global__ void __launch_bounds__(WT_WARPS * 32) clusters_warp_kernel(const floa
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
   const int d4 = dpad / 4;
   for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + wib; t < total; t += nwarps) {
-    // the cluster of task t: the last c with task_offs[c] <= t
+    // the cluster of task t: the last position with task_offs <= t
     int lo = 0, hi = n_clusters - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
       if (task_offs[mid] <= t) lo = mid;
       else hi = mid - 1;
     }
-    const int c = lo;
-    const uint32_t qb = q_offs[c] + 4u * (t - task_offs[c]);
+    const int at = lo;
+    const int c = static_cast<int>(cl_order[at]);
+    const uint32_t qb = q_offs[c] + 4u * (t - task_offs[at]);
     const int nqg = static_cast<int>(min(4u, q_offs[c + 1] - qb));
     const int r0 = static_cast<int>(row_offs[c]), r1 = static_cast<int>(row_offs[c + 1]);
     __syncwarp();  // the previous task's buffers are no longer read
@@ -782,7 +785,8 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
         return e;                                                                                        \
       w_<<<std::max(1, per_sm) * sms, WT_WARPS * 32, wsm, s>>>(queries, dim, dpad, ix->d_entry_rows,    \
                                                              ix->d_entry_ids, ix->d_offsets, q_offs, q_list, \
-                                                             task_offs, coarse, np, part_d, part_i);    \
+                                                             task_offs, ix->d_cl_order, coarse, np, part_d,   \
+                                                             part_i);                                   \
       merge_starts_kernel<NS><<<(nq + 255) / 256, 256, 0, s>>>(part_d, part_i, nq, np, ns, out);         \
       break;                                                                                             \
     }                                                                                                    \
@@ -816,7 +820,7 @@ cudaError_t launch_2level(song_index *ix, const float *queries, int nq, uint32_t
       default: SONG_HEADS_BY_NP(SONG_METRIC_COS); break;
     }
   }
-  cluster_scan_kernel<<<1, 1024, 0, s>>>(ix->d_cl_count, coarse, q_offs, cursor, task_offs);
+  cluster_scan_kernel<<<1, 1024, 0, s>>>(ix->d_cl_count, coarse, ix->d_cl_order, q_offs, cursor, task_offs);
   cluster_scatter_kernel<<<static_cast<unsigned>(std::min<size_t>((pairs + 255) / 256, 4096)), 256, 0, s>>>(
       probes, static_cast<int>(pairs), cursor, q_list);
   switch (ix->dx.metric) {
@@ -839,6 +843,7 @@ void clear_entries(song_index *ix) {
   cudaFree(ix->d_coarse_rows);
   cudaFree(ix->d_offsets);
   cudaFree(ix->d_cl_count);
+  cudaFree(ix->d_cl_order);
   cudaFree(ix->d_entry_work);
   cudaFree(ix->d_head_n2);
   cudaFree(ix->d_head_scores);
@@ -851,6 +856,7 @@ void clear_entries(song_index *ix) {
   ix->d_coarse_rows = nullptr;
   ix->d_offsets = nullptr;
   ix->d_cl_count = nullptr;
+  ix->d_cl_order = nullptr;
   ix->d_entry_work = nullptr;
   ix->cap_entry_work = 0;
   ix->n_entries = 0;
@@ -1024,6 +1030,13 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
     }
   }
   for (int k = 0; k < coarse; ++k) cperm[k] = static_cast<uint32_t>(corder[k]);
+  // the clusters largest first: the cluster phase's warps take tasks in this
+  // order, so that the long tasks start first and the last ones are short
+  std::vector<uint32_t> by_size(static_cast<size_t>(coarse));
+  for (int k = 0; k < coarse; ++k) by_size[k] = static_cast<uint32_t>(k);
+  std::stable_sort(by_size.begin(), by_size.end(), [&](uint32_t a, uint32_t b) {
+    return offsets[a + 1] - offsets[a] > offsets[b + 1] - offsets[b];
+  });
   // 3. device copies: entries in cluster order, coarse rows by id, offsets
   uint32_t *d_cperm = nullptr;
   if (e == cudaSuccess) e = song::dev_malloc(&d_perm, sizeof(uint32_t) * count);
@@ -1032,6 +1045,9 @@ extern "C" int song_index_set_entries_2level(song_index *ix, const uint64_t *ids
   if (e == cudaSuccess) e = song::dev_malloc(&ix->d_entry_ids, sizeof(uint32_t) * count);
   if (e == cudaSuccess) e = song::dev_malloc(&ix->d_coarse_rows, sizeof(float) * static_cast<size_t>(coarse) * dpad);
   if (e == cudaSuccess) e = song::dev_malloc(&ix->d_offsets, sizeof(uint32_t) * (coarse + 1));
+  if (e == cudaSuccess) e = song::dev_malloc(&ix->d_cl_order, sizeof(uint32_t) * coarse);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(ix->d_cl_order, by_size.data(), sizeof(uint32_t) * coarse, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_perm, perm.data(), sizeof(uint32_t) * count, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_cperm, cperm.data(), sizeof(uint32_t) * coarse, cudaMemcpyHostToDevice, ix->stream);
   if (e == cudaSuccess)

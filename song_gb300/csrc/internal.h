@@ -157,6 +157,7 @@ struct song_index {
   float *d_coarse_rows = nullptr;
   uint32_t *d_offsets = nullptr;
   uint32_t *d_cl_count = nullptr;      // probes per cluster (per call)
+  uint32_t *d_cl_order = nullptr;      // clusters by descending size (the cluster phase's task order)
   // head phase on the tensor cores (head_mma.cu): tensor map of the coarse
   // rows (a CUtensorMap), their squared norms, the per-chunk score buffer
   unsigned char head_map[128] = {};
