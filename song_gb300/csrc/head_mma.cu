@@ -30,6 +30,7 @@
 // distance formula by 2^-15 of its magnitude, far above its rounding.  A GPU
 // test measures the actual error against the bound.
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -262,7 +263,8 @@ struct HeadScoreArgs {
   int q_row0;
   int n_heads;
   int kchunks;   // ceil(dim / HM_K)
-  float *out;    // rows x ld: the lower bounds (OUT_BOUNDS) or the raw scores (OUT_RAW)
+  float *out;    // OUT_RAW: rows x ld raw scores
+  uint16_t *lo16;  // OUT_BOUNDS: rows x ld lower bounds, BF16 rounded down (ld a multiple of 8)
   int ld;
   float *tile_hi;       // OUT_BOUNDS: rows x tiles x NP smallest upper bounds of each head tile
   const float *q_n2;    // squared norms of all queries (OUT_BOUNDS)
@@ -276,8 +278,9 @@ constexpr int OUT_RAW = 0, OUT_BOUNDS = 1;
 
 // One 128 x 128 tile (blockIdx.x: queries, blockIdx.y: heads).  OUT_RAW
 // writes s~[q][h]; OUT_BOUNDS writes the lower bound of every head's search
-// distance (+inf past the last head) and, per query, the NP smallest upper
-// bounds of the tile.
+// distance (+inf past the last head) in BF16 rounded toward -inf -- still a
+// lower bound, in half the bytes, so that a whole batch's bounds stay in L2
+// -- and, per query, the NP smallest upper bounds of the tile.
 template <int METRIC, int NP, int OUT>
 __global__ void __launch_bounds__(128, 1)
     head_scores_kernel(const __grid_constant__ CUtensorMap tq, const __grid_constant__ CUtensorMap th,
@@ -404,7 +407,7 @@ __global__ void __launch_bounds__(128, 1)
           }
         }
       }
-      if (live && col0 < a.ld) {
+      if (OUT == OUT_RAW && live && col0 < a.ld) {
         float *dst = a.out + static_cast<size_t>(row) * a.ld + col0;
         if (col0 + 32 <= a.ld) {
 #pragma unroll
@@ -413,6 +416,23 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
           for (int i = 0; i < 32; ++i)
             if (col0 + i < a.ld) dst[i] = o[i];
+        }
+      }
+      if (OUT == OUT_BOUNDS && live && col0 < a.ld) {
+        uint16_t b[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) b[i] = __bfloat16_as_ushort(__float2bfloat16_rd(o[i]));
+        uint16_t *dst = a.lo16 + static_cast<size_t>(row) * a.ld + col0;
+        if (col0 + 32 <= a.ld) {
+#pragma unroll
+          for (int i = 0; i < 32; i += 8)
+            *reinterpret_cast<uint4 *>(dst + i) =
+                make_uint4(b[i] | (static_cast<uint32_t>(b[i + 1]) << 16), b[i + 2] | (static_cast<uint32_t>(b[i + 3]) << 16),
+                           b[i + 4] | (static_cast<uint32_t>(b[i + 5]) << 16), b[i + 6] | (static_cast<uint32_t>(b[i + 7]) << 16));
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i)
+            if (col0 + i < a.ld) dst[i] = b[i];
         }
       }
     }
@@ -431,12 +451,12 @@ __global__ void __launch_bounds__(128, 1)
 
 // One warp per query: probe_out[q * probes ..] = its `probes` nearest heads
 // (positions), ascending by (distance, position); cl_count counts probes per
-// head.  lo: rows x ld lower bounds (+inf past the heads); tile_hi: rows x
-// tiles x NP.  stats (or null): [0] queries, [1] heads re-scored, [2] full
-// scans.
+// head.  lo16: rows x ld lower bounds in BF16 (+inf past the heads); tile_hi:
+// rows x tiles x NP.  stats (or null): [0] queries, [1] heads re-scored, [2]
+// full scans.
 template <int METRIC, int NP>
 __global__ void __launch_bounds__(HM_SEL_WARPS * 32)
-    head_select_kernel(const float *queries, int dim, int q_row0, int rows, const float *lo_buf, int ld,
+    head_select_kernel(const float *queries, int dim, int q_row0, int rows, const uint16_t *lo16, int ld,
                        const float *tile_hi, int tiles, const float *heads, int dpad, int n_heads, int probes,
                        uint32_t *probe_out, uint32_t *cl_count, unsigned long long *stats) {
   __shared__ uint32_t cand[HM_SEL_WARPS][HM_CAP];
@@ -466,29 +486,29 @@ __global__ void __launch_bounds__(HM_SEL_WARPS * 32)
       warp_take<NP>(hb, hid, hp, U, wid);
     }
   }
-  // the shortlist: every head whose lower bound is <= U, eight float4 of
-  // bounds per lane in flight
-  const float4 *lo4 = reinterpret_cast<const float4 *>(lo_buf + static_cast<size_t>(r) * ld);
-  const int n4 = ld / 4;
+  // the shortlist: every head whose lower bound is <= U, four 16-byte
+  // groups of eight BF16 bounds per lane in flight
+  const uint4 *lo8 = reinterpret_cast<const uint4 *>(lo16 + static_cast<size_t>(r) * ld);
+  const int n8 = ld / 8;
   int count = 0;
-  for (int i0 = 0; i0 < n4; i0 += 32 * 8) {
-    float4 v[8];
+  for (int i0 = 0; i0 < n8; i0 += 32 * 4) {
+    uint4 v[4];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < 4; ++k) {
       const int i = i0 + 32 * k + lane;
-      v[k] = i < n4 ? __ldg(lo4 + i) : make_float4(__int_as_float(0x7f800000), __int_as_float(0x7f800000),
-                                                    __int_as_float(0x7f800000), __int_as_float(0x7f800000));
+      v[k] = i < n8 ? __ldg(lo8 + i) : make_uint4(0x7f807f80u, 0x7f807f80u, 0x7f807f80u, 0x7f807f80u);  // +inf
     }
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const float e[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t wds[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const bool f = e[c] <= U;
+      for (int c = 0; c < 8; ++c) {
+        const uint32_t bits = (c & 1) ? (wds[c >> 1] & 0xffff0000u) : (wds[c >> 1] << 16);
+        const bool f = __uint_as_float(bits) <= U;  // a BF16 value widened exactly
         const unsigned b = __ballot_sync(FULL, f);
         if (f) {
           const int pos = count + __popc(b & ((1u << lane) - 1u));
-          if (pos < HM_CAP) cand[w][pos] = static_cast<uint32_t>(4 * (i0 + 32 * k + lane) + c);
+          if (pos < HM_CAP) cand[w][pos] = static_cast<uint32_t>(8 * (i0 + 32 * k + lane) + c);
         }
         count += __popc(b);
       }
@@ -591,7 +611,7 @@ cudaError_t launch_chunk(const CUtensorMap &tq, const CUtensorMap &th, HeadScore
   kern<<<dim3((a.rows + HM_B - 1) / HM_B, tiles), 128, HM_SMEM, s>>>(tq, th, a);
   const int dpad = static_cast<int>(ix->dx.f32_row_bytes / 4);
   head_select_kernel<METRIC, NP><<<(a.rows + HM_SEL_WARPS - 1) / HM_SEL_WARPS, HM_SEL_WARPS * 32, 0, s>>>(
-      queries, ix->dx.dim, a.q_row0, a.rows, a.out, a.ld, a.tile_hi, tiles, ix->d_coarse_rows, dpad, ix->n_coarse,
+      queries, ix->dx.dim, a.q_row0, a.rows, a.lo16, a.ld, a.tile_hi, tiles, ix->d_coarse_rows, dpad, ix->n_coarse,
       np, probe_out, ix->d_cl_count, ix->head_stats_on ? ix->d_head_stats : nullptr);
   return cudaGetLastError();
 }
@@ -630,12 +650,16 @@ cudaError_t launch_heads_mma(song_index *ix, const float *queries, int nq, int n
   std::memcpy(&th, ix->head_map, sizeof th);
   const int NPsel = np <= 1 ? 1 : (np <= 2 ? 2 : (np <= 4 ? 4 : 8));
   const int tiles = (coarse + HM_B - 1) / HM_B;
-  // bounds of up to `chunk` queries at a time: about 32 MB, which stays in L2
-  const int ld = (coarse + 3) & ~3;
+  // BF16 bounds of up to `chunk` queries at a time: at most 96 MB, which
+  // stays in L2 between the two kernels (the whole batch at the headline)
+  const int ld = (coarse + 7) & ~7;
   const int chunk = std::max(HM_B, std::min((nq + HM_B - 1) / HM_B * HM_B,
-                                            static_cast<int>((32u << 20) / (4u * ld)) / HM_B * HM_B));
-  // work area: query norms (nq), bounds (chunk x ld), tile lists (chunk x tiles x 8)
-  const size_t need = static_cast<size_t>(nq) + static_cast<size_t>(chunk) * ld + static_cast<size_t>(chunk) * tiles * 8;
+                                            static_cast<int>((96u << 20) / (2u * ld)) / HM_B * HM_B));
+  // work area (256-byte aligned parts): query norms, bounds, tile lists
+  auto up256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t off_lo = up256(sizeof(float) * static_cast<size_t>(nq));
+  const size_t off_hi = off_lo + up256(sizeof(uint16_t) * static_cast<size_t>(chunk) * ld);
+  const size_t need = (off_hi + sizeof(float) * static_cast<size_t>(chunk) * tiles * 8 + 3) / 4;  // floats
   if (need > ix->cap_head_scores) {
     cudaFree(ix->d_head_scores);
     ix->d_head_scores = nullptr;
@@ -644,21 +668,10 @@ cudaError_t launch_heads_mma(song_index *ix, const float *queries, int nq, int n
     if (e != cudaSuccess) return e;
     ix->cap_head_scores = need;
   }
+  unsigned char *work = reinterpret_cast<unsigned char *>(ix->d_head_scores);
   float *q_n2 = ix->d_head_scores;
-  float *bounds = q_n2 + ((static_cast<size_t>(nq) + 3) & ~size_t(3));  // 16-byte aligned rows
-  float *tile_hi = bounds + static_cast<size_t>(chunk) * ld;
-  if (static_cast<size_t>(tile_hi - ix->d_head_scores) + static_cast<size_t>(chunk) * tiles * 8 > ix->cap_head_scores) {
-    // the alignment padding of q_n2 (at most 3 floats) did not fit: grow once more
-    cudaFree(ix->d_head_scores);
-    ix->d_head_scores = nullptr;
-    ix->cap_head_scores = 0;
-    cudaError_t e = song::dev_malloc(&ix->d_head_scores, sizeof(float) * (need + 4));
-    if (e != cudaSuccess) return e;
-    ix->cap_head_scores = need + 4;
-    q_n2 = ix->d_head_scores;
-    bounds = q_n2 + ((static_cast<size_t>(nq) + 3) & ~size_t(3));
-    tile_hi = bounds + static_cast<size_t>(chunk) * ld;
-  }
+  uint16_t *bounds = reinterpret_cast<uint16_t *>(work + off_lo);
+  float *tile_hi = reinterpret_cast<float *>(work + off_hi);
   row_norms_kernel<<<(nq + 7) / 8, 256, 0, s>>>(queries, nq, dim, dim, q_n2);
   for (int q0 = 0; q0 < nq; q0 += chunk) {
     HeadScoreArgs a;
@@ -666,7 +679,8 @@ cudaError_t launch_heads_mma(song_index *ix, const float *queries, int nq, int n
     a.q_row0 = q0;
     a.n_heads = coarse;
     a.kchunks = (dim + HM_K - 1) / HM_K;
-    a.out = bounds;
+    a.out = nullptr;
+    a.lo16 = bounds;
     a.ld = ld;
     a.tile_hi = tile_hi;
     a.q_n2 = q_n2;
@@ -712,6 +726,7 @@ cudaError_t launch_head_scores_only(song_index *ix, const float *queries, int nq
   a.n_heads = ix->n_coarse;
   a.kchunks = (dim + HM_K - 1) / HM_K;
   a.out = scores;
+  a.lo16 = nullptr;
   a.ld = ld;
   a.error = ix->d_error;
   a.wait_limit = ix->wait_limit;
