@@ -841,13 +841,13 @@ def pq_table(torch, ix, dq, stream, flush, data, queries, kth10, kth100, w, targ
 def entry_launches(args, w, nq):
     """Kernels of one entry choice: flat, one; two-level, the query norms and
     a score + select pair per chunk of queries (tensor-core heads, dims a
-    multiple of 4: a chunk's bounds take at most 32 MB, in 128-query tiles)
-    or one head kernel, then scan, scatter, cluster and merge kernels."""
+    multiple of 4: a chunk's BF16 bounds take at most 96 MB, in 128-query
+    tiles) or one head kernel, then scan, scatter, cluster and merge kernels."""
     if args.coarse <= 0:
         return 1
     if w.dim % 4 == 0:
-        ld = (args.coarse + 3) // 4 * 4
-        chunk = max(128, min((nq + 127) // 128 * 128, (32 << 20) // (4 * ld) // 128 * 128))
+        ld = (args.coarse + 7) // 8 * 8
+        chunk = max(128, min((nq + 127) // 128 * 128, (96 << 20) // (2 * ld) // 128 * 128))
         heads = 1 + 2 * ((nq + chunk - 1) // chunk)
     else:
         heads = 1
