@@ -212,21 +212,23 @@ __device__ __forceinline__ void warp_take(const float (&bd)[N], const uint32_t (
 }
 
 // Exact search distance (lane-strided FMA chain over dims, xor butterfly) of
-// the query to 32 head rows at once: row r is rows + idx(r) * dpad; lane l
-// returns row l's distance.  Products taken two rows at a time through the
-// paired FP32 instructions (the scalar roundings, in the scalar order).
-template <int METRIC, class Idx>
-__device__ __forceinline__ float rows32_distance(const float *qv, int dim, const float *rows, int dpad, Idx idx,
-                                                 int lane) {
+// the query to R head rows at once (R = 8 or 32): row r is rows + idx(r) *
+// dpad; lane l returns row l / (32 / R)'s distance.  Products taken two rows
+// at a time through the paired FP32 instructions (the scalar roundings, in
+// the scalar order); the R rows meet in one transposed butterfly.
+template <int METRIC, int R, class Idx>
+__device__ __forceinline__ float rows_distance(const float *qv, int dim, const float *rows, int dpad, Idx idx,
+                                               int lane) {
   constexpr bool COS = METRIC == SONG_METRIC_COS;
-  uint64_t acc[16], ln[16];
+  constexpr int P = R / 2;
+  uint64_t acc[P], ln[P];
 #pragma unroll
-  for (int p = 0; p < 16; ++p) acc[p] = ln[p] = 0ull;
+  for (int p = 0; p < P; ++p) acc[p] = ln[p] = 0ull;
   for (int j = lane; j < dim; j += 32) {
     const float qj = qv[j];
     const uint64_t qq = f2_pack(qj, qj);
 #pragma unroll
-    for (int p = 0; p < 16; ++p) {
+    for (int p = 0; p < P; ++p) {
       const float x0 = __ldg(rows + static_cast<size_t>(idx(2 * p)) * dpad + j);
       const float x1 = __ldg(rows + static_cast<size_t>(idx(2 * p + 1)) * dpad + j);
       const uint64_t xx = f2_pack(x0, x1);
@@ -239,16 +241,16 @@ __device__ __forceinline__ float rows32_distance(const float *qv, int dim, const
       }
     }
   }
-  float v[32];
+  float v[R];
 #pragma unroll
-  for (int p = 0; p < 16; ++p) f2_unpack(acc[p], v[2 * p], v[2 * p + 1]);
-  const float t = butterfly_rows<32>(v, lane);
+  for (int p = 0; p < P; ++p) f2_unpack(acc[p], v[2 * p], v[2 * p + 1]);
+  const float t = butterfly_rows<R>(v, lane);
   if (METRIC == SONG_METRIC_L2) return t;
   if (METRIC == SONG_METRIC_IP) return -t;
-  float lv[32];
+  float lv[R];
 #pragma unroll
-  for (int p = 0; p < 16; ++p) f2_unpack(ln[p], lv[2 * p], lv[2 * p + 1]);
-  const float len = butterfly_rows<32>(lv, lane);
+  for (int p = 0; p < P; ++p) f2_unpack(ln[p], lv[2 * p], lv[2 * p + 1]);
+  const float len = butterfly_rows<R>(lv, lane);
   if (len != 0.0f) {
     const float sign = t < 0.0f ? 1.0f : -1.0f;
     return __fdiv_rn(__fmul_rn(__fmul_rn(sign, t), t), len);
@@ -527,16 +529,35 @@ __global__ void __launch_bounds__(HM_SEL_WARPS * 32)
   // finite, e.g. after a timed-out score kernel: scan everything then too)
   const bool full_scan = count > HM_CAP || count < probes;
   const int total = full_scan ? n_heads : count;
-  for (int g = 0; g < total; g += 32) {
-    const int n = min(32, total - g);
-    float d;
-    if (full_scan) {
-      d = rows32_distance<METRIC>(qv, dim, heads, dpad, [&](int i) { return min(g + i, n_heads - 1); }, lane);
+  // 32 rows per pass, the last few (the common shortlist of a handful of
+  // heads) 8 at a time: a pass reads every one of its rows
+  for (int g = 0; g < total;) {
+    const int left = total - g;
+    if (left > 8) {
+      const int n = min(32, left);
+      float d;
+      if (full_scan) {
+        d = rows_distance<METRIC, 32>(qv, dim, heads, dpad, [&](int i) { return min(g + i, n_heads - 1); }, lane);
+      } else {
+        const uint32_t *cl = cand[w] + g;
+        d = rows_distance<METRIC, 32>(qv, dim, heads, dpad, [&](int i) { return cl[min(i, n - 1)]; }, lane);
+      }
+      if (lane < n) best_insert<NP>(bd, bi, d, full_scan ? static_cast<uint32_t>(g + lane) : cand[w][g + lane]);
+      g += n;
     } else {
-      const uint32_t *cl = cand[w] + g;
-      d = rows32_distance<METRIC>(qv, dim, heads, dpad, [&](int i) { return cl[min(i, n - 1)]; }, lane);
+      const int n = left;
+      float d;
+      if (full_scan) {
+        d = rows_distance<METRIC, 8>(qv, dim, heads, dpad, [&](int i) { return min(g + i, n_heads - 1); }, lane);
+      } else {
+        const uint32_t *cl = cand[w] + g;
+        d = rows_distance<METRIC, 8>(qv, dim, heads, dpad, [&](int i) { return cl[min(i, n - 1)]; }, lane);
+      }
+      const int row = lane >> 2;  // lane l holds row l / 4
+      if ((lane & 3) == 0 && row < n)
+        best_insert<NP>(bd, bi, d, full_scan ? static_cast<uint32_t>(g + row) : cand[w][g + row]);
+      g += n;
     }
-    if (lane < n) best_insert<NP>(bd, bi, d, full_scan ? static_cast<uint32_t>(g + lane) : cand[w][g + lane]);
   }
   int hp = 0;
   for (int k = 0; k < probes; ++k) {
