@@ -54,8 +54,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PQ_SWEEP = [40, 45, 50, 55, 60, 65, 70, 75, 80, 90, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400, 500, 600, 800,
-            1000]
+PQ_SWEEP = list(range(40, 50)) + [50, 55, 60, 65, 70, 75, 80, 90, 100, 125, 150, 175, 200, 225, 250, 300, 350, 400,
+                                  500, 600, 800, 1000]
 PQ_TABLE = [50, 75, 100, 150, 200, 250, 300, 400]   # the reported sweep (top-10; top-100 from pq 100)
 CPU_K_SWEEP = [10, 20, 40, 80, 150, 300, 500, 800, 1200, 1600, 2000]
 REF_GPU_PQ = [100, 200, 400, 600, 800, 1000]         # pq values of the rebuilt reference kernel
