@@ -21,7 +21,11 @@
 // reference does, unless SONG_ENTRIES > 0: then each query starts from its
 // SONG_STARTS (default 4) nearest of SONG_ENTRIES vertices drawn with seed
 // SONG_ENTRY_SEED (default 11); SONG_COARSE > 0 makes the choice two-level
-// with SONG_PROBES (default 4) clusters probed.
+// with SONG_PROBES (default 4) clusters probed.  SONG_N_MULTIPROBE,
+// SONG_FINISH_CNT and SONG_MULTIPROBE_DOUBLE_CHECK set the kernel's
+// multi-probe knobs, which the reference fixes at build time
+// (warp_astar_accelerator.h:29-30,307; fill_parameters.sh:36-37); defaults
+// 1, 1 and 0, the reference's.
 //
 // Binary I/O (no reference counterpart; the reference parses LIBSVM text,
 // parser.h:48-64): SONG_DATA_FORMAT=f32 makes build read <build_data> and
@@ -276,6 +280,16 @@ int main(int argc, char **argv) {
       rc = coarse > 0 ? song_index_set_entries_2level(ix, ent.data(), static_cast<int>(ent.size()), coarse,
                                                       env_int("SONG_PROBES", 4), env_int("SONG_STARTS", 4))
                       : song_index_set_entries(ix, ent.data(), static_cast<int>(ent.size()), env_int("SONG_STARTS", 4));
+      if (rc) {
+        fprintf(stderr, "%s: %s\n", song_status_string(rc), song_last_error());
+        song_index_free(ix);
+        return 1;
+      }
+    }
+    const int probes = env_int("SONG_N_MULTIPROBE", 1), finish_cnt = env_int("SONG_FINISH_CNT", 1);
+    const int double_check = env_int("SONG_MULTIPROBE_DOUBLE_CHECK", 0);
+    if (probes != 1 || finish_cnt != 1 || double_check != 0) {
+      rc = song_index_set_multiprobe(ix, probes, finish_cnt, double_check);
       if (rc) {
         fprintf(stderr, "%s: %s\n", song_status_string(rc), song_last_error());
         song_index_free(ix);

@@ -87,3 +87,28 @@ def test_cli_binary_queries_and_results(song, oracle, tmp_path):
     o_ids = np.asarray(ox.kernel_search(queries, pq, oracle.MODE_LEX)[0], dtype=np.uint64)
     assert np.array_equal(got[:, :pq], o_ids[:, :pq])
     assert np.all(got[:, pq:] == np.uint64(0xFFFFFFFFFFFFFFFF))
+
+
+def test_cli_multiprobe_knobs(song, oracle, tmp_path):
+    """SONG_N_MULTIPROBE / SONG_FINISH_CNT / SONG_MULTIPROBE_DOUBLE_CHECK: the
+    knobs the reference compiles in, here per run; the oracle's ids under the
+    same knobs."""
+    g = load_golden("l2_s5_d32")
+    data, queries = g["data"], g["queries"]
+    data.astype(np.float32).tofile(str(tmp_path / "bfsg.data"))
+    g["graph"].astype(np.uint64).tofile(str(tmp_path / "bfsg.graph"))
+    write_libsvm(str(tmp_path / "q.libsvm"), queries)
+    pq, show = 50, 10
+    ox = oracle.OracleIndex(data, g["graph"], int(g["shift"]), int(g["metric"]))
+    for probes, fc, dc in ((2, 1, 1), (3, 2, 0)):
+        r = _run(["test", "0", "q.libsvm", str(pq), str(data.shape[0]), str(data.shape[1]), str(show), "l2"],
+                 tmp_path, SONG_N_MULTIPROBE=probes, SONG_FINISH_CNT=fc, SONG_MULTIPROBE_DOUBLE_CHECK=dc)
+        assert r.returncode == 0, r.stderr
+        o_ids = ox.kernel_search(queries, pq, oracle.MODE_LEX, probes=probes, finish_cnt=fc,
+                                 double_check=bool(dc))[0]
+        lines = r.stdout.strip("\n").split("\n")
+        for i, line in enumerate(lines):
+            assert [int(x) for x in line.split()] == [int(x) for x in o_ids[i, :show]], (probes, fc, dc, i)
+    r = _run(["test", "0", "q.libsvm", str(pq), str(data.shape[0]), str(data.shape[1]), str(show), "l2"],
+             tmp_path, SONG_N_MULTIPROBE=9)
+    assert r.returncode != 0 and "probes" in r.stderr
